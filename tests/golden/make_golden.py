@@ -1,0 +1,227 @@
+"""Generate the golden vectors that pin the oracle to lentil 0.8.8 itself.
+
+Runs lentil from its source tree (read-only) on seeded inputs and writes
+small ``.npz`` fixtures next to this script.  The reference package cannot
+travel to the GPU machine, so the fixtures are committed and the tests only
+read them.
+
+Usage (in a checkout that has the lentil sources):
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def main(ref_root):
+    sys.dont_write_bytecode = True
+    sys.path.insert(0, ref_root)
+    import lentil
+    import lentil.field
+    import lentil.fourier
+    import lentil.helper
+    import lentil.radiometry
+
+    rng = np.random.default_rng(20261203)
+
+    def crand(*shape):
+        return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+    # ---------------------------------------------------------------- dft2
+    d = {}
+    cases = [
+        # name, f shape, alpha, shape, shift, offset, unitary
+        ('even10', (10, 10), 1 / 10, None, (0, 0), (0, 0), False),
+        ('odd11', (11, 11), 1 / 11, None, (0, 0), (0, 0), False),
+        ('rect10x11', (10, 11), (1 / 10, 1 / 11), None, (0, 0), (0, 0), False),
+        ('general', (23, 17), (0.013, 0.021), (31, 29), (2.3, -1.7), (3, -2), True),
+        ('floatoff', (16, 20), (0.011, 0.017), (24, 18), (-3.0, 4.0), (0.5, -1.25), True),
+        ('wide', (64, 64), 1 / 200, (96, 80), (0.25, -0.75), (0, 0), True),
+        ('negalpha', (12, 9), (-0.05, 0.03), (13, 15), (1.0, 0.0), (-2, 1), True),
+        ('big', (128, 96), (1.3e-3, 2.1e-3), (160, 144), (5.5, -7.25), (-11, 6), True),
+    ]
+    names = []
+    for name, fs, alpha, shape, shift, offset, unitary in cases:
+        f = crand(*fs)
+        F = lentil.fourier.dft2(f, alpha, shape=shape, shift=shift, offset=offset,
+                                unitary=unitary)
+        d[f'{name}_f'] = f
+        d[f'{name}_F'] = F
+        d[f'{name}_alpha'] = np.broadcast_to(alpha, (2,)).astype(float)
+        d[f'{name}_shape'] = np.asarray(F.shape)
+        d[f'{name}_shift'] = np.asarray(shift, float)
+        d[f'{name}_offset'] = np.asarray(offset, float)
+        d[f'{name}_unitary'] = np.asarray(unitary)
+        names.append(name)
+    # integer shift moves the centroid exactly (tests/test_fourier.py:68-78)
+    n = 100
+    shift = np.array([7.0, -12.0])
+    d['shift100_F'] = lentil.fourier.dft2(np.ones((n, n)), 1 / n, shift=shift)
+    d['shift100_shift'] = shift
+    # sliced + offset == full (tests/test_fourier.py:81-94)
+    f = np.zeros((10, 10), dtype=complex)
+    f[4:7, 2:5] = crand(3, 3)
+    slc = lentil.helper.boundary_slice(f)
+    d['offset_f'] = f
+    d['offset_slice'] = np.array([slc[0].start, slc[0].stop, slc[1].start, slc[1].stop])
+    d['offset_offset'] = np.asarray(lentil.helper.slice_offset(slc, f.shape))
+    d['offset_F'] = lentil.fourier.dft2(f, alpha=1 / 3, shape=10)
+    # idft2
+    for name, n in (('ieven', 10), ('iodd', 11)):
+        F = crand(n, n)
+        d[f'{name}_F'] = F
+        d[f'{name}_f'] = lentil.fourier.idft2(F, 1 / n, unitary=False)
+    d['names'] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, 'dft2.npz'), **d)
+
+    # ---------------------------------------------------------- propagate
+    p = {}
+
+    def pupil(shape, radius, coeffs, focal_length=10, diameter=1, antialias=True):
+        amp = lentil.normalize_power(lentil.circle(shape, radius, antialias=antialias))
+        opd = lentil.zernike_compose(amp, coeffs) if coeffs is not None else 0
+        return lentil.Pupil(amplitude=amp, opd=opd, pixelscale=diameter / (2 * radius),
+                            focal_length=focal_length), amp, opd
+
+    def run(name, pl, amp, opd, mask3d=None, wl=650e-9, fit_tilt=False, **kw):
+        # fit_tilt may modify the OPD array in place: keep the input as given
+        opd = np.array(np.broadcast_to(np.asarray(pl.opd, float), np.shape(amp)), copy=True)
+        if fit_tilt:
+            pl.fit_tilt(inplace=True)
+        w = lentil.Wavefront(wl) * pl
+        w = lentil.propagate_dft(w, **kw)
+        p[f'{name}_amp'] = np.asarray(amp, float)
+        p[f'{name}_opd'] = opd
+        if mask3d is not None:
+            p[f'{name}_mask'] = np.asarray(mask3d, float)
+        p[f'{name}_pixelscale_in'] = np.asarray(pl.pixelscale, float)
+        p[f'{name}_focal_length'] = np.asarray(pl.focal_length, float)
+        p[f'{name}_wavelength'] = np.asarray(wl, float)
+        p[f'{name}_fit_tilt'] = np.asarray(fit_tilt)
+        for k in ('pixelscale', 'shape', 'prop_shape', 'oversample'):
+            v = kw.get(k)
+            p[f'{name}_{k}'] = np.asarray(-1 if v is None else v)
+        if 'mask' in kw:
+            p[f'{name}_outmask'] = np.asarray(kw['mask'], float)
+        p[f'{name}_intensity'] = w.intensity
+        p[f'{name}_nfields'] = np.asarray(len(w.data))
+        return w
+
+    # config-1 workload: 256^2 circle (non-antialiased), Noll 2-11 ~ N(0, 20 nm)
+    c = np.concatenate([[0.0], rng.normal(0, 20e-9, 10)])
+    amp = lentil.normalize_power(lentil.circle((256, 256), 128, antialias=False))
+    opd = lentil.zernike_compose(amp, c)
+    pl = lentil.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 256, focal_length=10)
+    run('config1', pl, amp, opd, pixelscale=5e-6, shape=128, oversample=2)
+
+    # tilt with and without fit_tilt (tests/test_propagate.py:45-131)
+    coeffs = [0, 2.1e-6, -1.3e-6]
+    for ft in (False, True):
+        pl, amp, opd = pupil((128, 128), 60, coeffs)
+        run(f'tilt_fit{int(ft)}', pl, amp, opd, fit_tilt=ft, pixelscale=5e-6,
+            shape=48, oversample=3)
+    # output mask (tests/test_propagate_mask.py)
+    pl, amp, opd = pupil((128, 128), 60, [0, 1e-7, 2e-7, 5e-8])
+    mask = lentil.rectangle((128, 128), 48, 40, shift=(10, -15), antialias=False)
+    run('outmask', pl, amp, opd, pixelscale=5e-6, shape=64, oversample=2, mask=mask)
+    # everything tilted out of the window (tests/test_propagate.py:134-141)
+    pl, amp, opd = pupil((127, 127), 60, [0, 1e-3])
+    run('nooutput', pl, amp, opd, fit_tilt=True, pixelscale=5e-6, shape=32, oversample=2)
+    # prop_shape < shape, odd shapes, rectangular output
+    pl, amp, opd = pupil((101, 99), 45, [0, 3e-7, -2e-7, 1e-7, 4e-8])
+    run('oddrect', pl, amp, opd, pixelscale=4e-6, shape=(45, 37), prop_shape=(21, 17),
+        oversample=3)
+    # segmented aperture: 3-D mask, per-segment fields, with and without fit_tilt
+    segs = lentil.hex_segments(rings=1, seg_radius=14, seg_gap=2)
+    H = segs.shape[1]
+    gmask = np.sum(segs, axis=0)
+    amp = lentil.normalize_power(gmask)
+    opd = np.zeros_like(amp)
+    for k in range(segs.shape[0]):
+        r, cc = lentil.helper.mesh(amp.shape)
+        ptt = rng.normal(0, 50e-9, 3)
+        opd += segs[k] * (ptt[0] + ptt[1] * r / H + ptt[2] * cc / H)
+    for ft in (False, True):
+        pl = lentil.Pupil(amplitude=amp, opd=opd, mask=segs, pixelscale=1 / H,
+                          focal_length=10)
+        run(f'seg_fit{int(ft)}', pl, amp, opd, mask3d=segs, fit_tilt=ft, wl=550e-9,
+            pixelscale=20e-6, shape=40, oversample=2)
+    # small broadband accumulation through Wavefront.insert
+    pl, amp, opd = pupil((64, 64), 30, [0, 0, 0, 5e-8, 2e-8])
+    wl = np.array([500e-9, 620e-9, 780e-9])
+    wt = np.array([0.2, 0.5, 0.3])
+    img = np.zeros((48, 48))
+    for lam, w8 in zip(wl, wt):
+        w = lentil.propagate_dft(lentil.Wavefront(lam) * pl, pixelscale=6e-6, shape=24,
+                                 oversample=2)
+        img = w.insert(img, weight=w8)
+    p['bb_amp'], p['bb_opd'], p['bb_wl'], p['bb_wt'], p['bb_img'] = amp, opd, wl, wt, img
+    p['bb_pixelscale_in'] = np.asarray(pl.pixelscale, float)
+    np.savez_compressed(os.path.join(HERE, 'propagate.npz'), **p)
+
+    # -------------------------------------------------------------- fields
+    fd = {}
+    a = lentil.field.Field(data=np.ones((5, 4)), pixelscale=1, offset=[-2, -2])
+    b = lentil.field.Field(data=np.ones((3, 3)), pixelscale=1, offset=[0, -1])
+    c = lentil.field.merge(a, b)
+    fd['merge_data'], fd['merge_offset'] = c.data, np.asarray(c.offset)
+    fs = [lentil.field.Field(data=crand(5, 6), pixelscale=1, offset=[0, 0]),
+          lentil.field.Field(data=crand(4, 4), pixelscale=1, offset=[2, 3]),
+          lentil.field.Field(data=crand(3, 3), pixelscale=1, offset=[20, 20]),
+          lentil.field.Field(data=crand(7, 2), pixelscale=1, offset=[-3, -4])]
+    for k, f in enumerate(fs):
+        fd[f'reduce_in{k}_data'], fd[f'reduce_in{k}_offset'] = f.data, np.asarray(f.offset)
+    red = lentil.field.reduce(fs)
+    fd['reduce_n'] = np.asarray(len(red))
+    for k, f in enumerate(red):
+        fd[f'reduce_out{k}_data'], fd[f'reduce_out{k}_offset'] = f.data, np.asarray(f.offset)
+    out = np.zeros((9, 8))
+    for f in fs:
+        out = lentil.field.insert(f, out, intensity=True, weight=0.7)
+    fd['insert_intensity'] = out
+    out = np.zeros((9, 8), dtype=complex)
+    for f in fs:
+        out = lentil.field.insert(f, out)
+    fd['insert_complex'] = out
+    np.savez_compressed(os.path.join(HERE, 'field.npz'), **fd)
+
+    # ------------------------------------------------------------ detector
+    dd = {}
+    for name, n, os_ in (('px64os2', 64, 2), ('px90os3', 90, 3), ('px128os4', 128, 4)):
+        img = rng.uniform(0, 1, (n, n)) ** 4
+        dd[f'{name}_img'] = img
+        dd[f'{name}_os'] = np.asarray(os_)
+        dd[f'{name}_pixel'] = lentil.detector.pixel(img, os_)
+        dd[f'{name}_pixelate'] = lentil.detector.pixelate(img, os_)
+    np.savez_compressed(os.path.join(HERE, 'detector.npz'), **dd)
+
+    # ---------------------------------------------------------- generators
+    g = {}
+    g['circle'] = lentil.circle((64, 70), 20.3, shift=(1.5, -2.25))
+    g['circle_noaa'] = lentil.circle((64, 64), 20, antialias=False)
+    g['hexagon'] = lentil.hexagon((64, 64), 20, shift=(2, -3))
+    g['hexagon_rot'] = lentil.hexagon((64, 64), 20, rotate=True)
+    g['rectangle'] = lentil.rectangle((64, 64), 30, 12, shift=(3, 4), angle=30)
+    g['spider'] = lentil.spider((64, 64), 3, angle=210)
+    g['hexseg'] = lentil.hex_segments(rings=2, seg_radius=10, seg_gap=1)
+    m = lentil.circle((64, 64), 30)
+    g['zcoeffs'] = rng.normal(0, 1e-7, 22)
+    g['zcompose'] = lentil.zernike_compose(m, g['zcoeffs'])
+    mm = g['hexseg'][4]
+    rho, theta = lentil.zernike_coordinates(mm)
+    g['zcoord_rho'], g['zcoord_theta'] = rho, theta
+    g['zcompose_seg'] = lentil.zernike_compose(mm, [1e-8, 2e-8, -3e-8], rho=rho, theta=theta)
+    g['psd'] = lentil.power_spectrum(m, 1 / 64, 25e-9, 8, 2, seed=7)
+    wl = np.linspace(500, 900, 64)
+    bb = lentil.radiometry.Blackbody(wl, 5800).value
+    g['bb_wl_nm'], g['bb_value'] = wl, bb
+    np.savez_compressed(os.path.join(HERE, 'generators.npz'), **g)
+    print('golden fixtures written to', HERE)
+
+
+if __name__ == '__main__':
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
