@@ -1,0 +1,391 @@
+"""Benchmark: polychromatic 1024^2 PSFs/s of the broadband segmented workload.
+
+Workload (one "step" = one batch of PSFs through the fused broadband plan):
+1024x1024 pupil of 18 hexagonal segments (two rings, empty centre, 2 px
+gaps), per-segment piston/tip/tilt ~ N(0, 50 nm), global Noll 2-22 ~
+N(0, 15 nm), 64 wavelengths over 500-900 nm weighted by a 5800 K blackbody,
+512x512 detector at oversample 2 (1024^2 field per wavelength).  Inputs are
+seeded synthetic arrays of those shapes.
+
+Arms:
+  default           the split-precision tensor-core plan (lentil_gb300) on cuda
+  --impl reference  lentil's own CPU algorithm (the numpy restatement under
+                    oracle/) on the host cores, bounded sample of wavelengths
+
+Prints ONE JSON line (rank 0).  Under torchrun every rank runs an independent
+replica on its own GPU (the path has no data exchange); value is the total
+PSFs of all ranks over the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'polychromatic 1024^2 PSFs/s (broadband segmented, 64 wavelengths), split precision'
+UNIT = 'PSFs/s'
+PEAKS_FILE = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+TRAFFIC_FILE = os.path.join(ROOT, 'profiles', 'mft_split_broadband_segmented.json')
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--batch', type=int, default=1, help='PSFs per step')
+    ap.add_argument('--precision', default='split-fp16',
+                    choices=['split-fp16', 'split-bf16', 'fp64'])
+    ap.add_argument('--fp64-steps', type=int, default=2,
+                    help='timed steps of the plain complex128 plan (0 to skip)')
+    ap.add_argument('--cpu-lambdas', type=int, default=2,
+                    help='wavelengths in the bounded CPU-baseline sample')
+    ap.add_argument('--npix', type=int, default=1024)
+    ap.add_argument('--wavelengths', type=int, default=64)
+    return ap.parse_args()
+
+
+def config_dict(wl, args, extra=None):
+    d = {'workload': 'broadband segmented PSF: 1024^2 pupil, 18 hex segments (2 rings, '
+                     'empty centre, 2 px gaps), per-segment PTT N(0,50nm), Noll 2-22 '
+                     'N(0,15nm), 64 wavelengths 500-900 nm, 5800 K blackbody, 512^2 '
+                     'detector x oversample 2',
+         'pupil': list(wl.plane_shape), 'wavelengths': len(wl.wavelengths),
+         'output': [wl.det_shape * wl.oversample] * 2, 'batch_psfs_per_step': args.batch,
+         'optics': 'D = 1 m over the pupil grid, f = 10 m, 5 um pixels',
+         'l2': 'working set (DFT matrices + per-wavelength operands, > 1 GB) exceeds the '
+               '129 MB L2; no flush needed'}
+    if extra:
+        d.update(extra)
+    return d
+
+
+# --------------------------------------------------------------------------
+# CPU reference: lentil's algorithm (numpy restatement) on the host cores
+# --------------------------------------------------------------------------
+def cpu_reference(wl, n_lambda, opd):
+    """Seconds per wavelength of lentil's user loop on a bounded sample."""
+    from oracle import lentil_oracle as lo
+    pupil = lo.Pupil(amplitude=wl.amp, opd=opd, mask=wl.mask3d, pixelscale=wl.pixelscale_in,
+                     focal_length=wl.focal_length)
+    idx = np.linspace(0, len(wl.wavelengths) - 1, n_lambda).round().astype(int)
+    t0 = time.perf_counter()
+    lo.broadband_psf(pupil, wl.wavelengths[idx], wl.weights[idx], wl.det_pixelscale,
+                     shape=wl.det_shape, oversample=wl.oversample)
+    dt = time.perf_counter() - t0
+    return dt / n_lambda, idx
+
+
+def run_reference(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    from lentil_gb300 import workloads
+    wl = workloads.broadband_segmented(args.npix, args.wavelengths)
+    opd = wl.opds(1)[0]
+    n = max(1, args.cpu_lambdas)
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_reference(wl, 1, opd)
+    per = []
+    for _ in range(args.steps):
+        s, _ = cpu_reference(wl, n, opd)
+        per.append(s)
+    t_psf = statistics.mean(per) * len(wl.wavelengths)
+    value = 1.0 / t_psf
+    cores = os.cpu_count()
+    line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': 0,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * t_psf,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic', 'config': config_dict(wl, args),
+            'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                             'sample': f'{n} of {len(wl.wavelengths)} wavelengths per step of '
+                                       'one PSF through lentil\'s per-segment user loop '
+                                       '(numpy restatement), extrapolated linearly'},
+            'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling while the timed region runs."""
+    Q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index, self.proc = index, None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), f'--query-gpu={self.Q}',
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, power, reasons = [], [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in getattr(self, 'lines', []):
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0])); smax.append(float(f[1])); power.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower() == 'active':
+                    reasons.add(name)
+        if not sm:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': [], 'samples': 0}
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(smax),
+                'power_w_max': max(power), 'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as fh:
+            d = json.load(fh)
+        return d, 'measured'
+    except (OSError, ValueError):
+        return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0, 'bf16_tflops_sustained': 1700.0}, 'fallback'
+
+
+def traffic_per_launch():
+    try:
+        with open(TRAFFIC_FILE) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return None
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    import lentil_gb300 as lg
+    from lentil_gb300 import _lib, broadband, workloads
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    wl = workloads.broadband_segmented(args.npix, args.wavelengths)
+    B = args.batch
+    gmask = wl.mask3d.sum(axis=0)
+    amp_eff = wl.amp * gmask                       # lentil: amplitude[s] * mask[s]
+    opd = wl.opds(B, seed=wl.seed + rank)
+    s = lg.util.boundary_slice(gmask)
+    geo = broadband.plan_geometry(wl.plane_shape, s, [], np.broadcast_to(wl.pixelscale_in, (2,)),
+                                  wl.focal_length, lg.pupil, wl.wavelengths, wl.det_pixelscale,
+                                  shape=wl.det_shape, oversample=wl.oversample)
+    L = len(geo.wavelengths)
+    dev = torch.device('cuda', local)
+    stream = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    plan = broadband.make_plan(geo, batch=B, precision=args.precision)
+    torch.cuda.synchronize()
+    plan_ms = 1e3 * (time.perf_counter() - t0)
+
+    A = torch.as_tensor(np.broadcast_to(amp_eff, (B,) + wl.plane_shape).copy(), device=dev)
+    O = torch.as_tensor(opd, device=dev)
+    Wt = torch.as_tensor(np.broadcast_to(wl.weights[geo.keep], (B, L)).copy(), device=dev)
+    out = torch.empty((B,) + geo.shape_out, dtype=torch.float64, device=dev)
+    lib = _lib.load()
+
+    # ---------------- device-resident timed region (value) ----------------
+    for _ in range(args.warmup):
+        plan.execute(A, O, Wt, out=out, check=False)
+    _lib.call('lgb_psf_plan_status', plan._h, stream.cuda_stream)
+    lib.lgb_psf_plan_profile(plan._h, 1)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            plan.execute(A, O, Wt, out=out, check=False)
+            ev[k][1].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    lib.lgb_psf_plan_profile(plan._h, 0)
+    import ctypes
+    kms = (ctypes.c_double * 4)()
+    kcnt = (ctypes.c_int * 4)()
+    _lib.call('lgb_psf_plan_kernel_times', plan._h, kms, kcnt, 4)
+    _lib.call('lgb_psf_plan_status', plan._h, stream.cuda_stream)
+    total_ms = t_start.elapsed_time(t_end)
+    step_ms = sorted(a.elapsed_time(b) for a, b in ev)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * B * args.steps / (total_ms / 1e3)
+
+    # ---------------- end-to-end through the plan with host buffers --------
+    hA = torch.empty_like(A, device='cpu').pin_memory()
+    hO = torch.empty_like(O, device='cpu').pin_memory()
+    hW = torch.empty_like(Wt, device='cpu').pin_memory()
+    hOut = torch.empty_like(out, device='cpu').pin_memory()
+    hA.copy_(A.cpu()); hO.copy_(O.cpu()); hW.copy_(Wt.cpu())
+    dA, dO, dW = torch.empty_like(A), torch.empty_like(O), torch.empty_like(Wt)
+
+    def e2e_step():
+        dA.copy_(hA, non_blocking=True)
+        dO.copy_(hO, non_blocking=True)
+        dW.copy_(hW, non_blocking=True)
+        plan.execute(dA, dO, dW, out=out, check=False)
+        hOut.copy_(out, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * B * args.steps / (e2e_ms / 1e3)
+    h2d = (A.numel() + O.numel() + Wt.numel()) * 8
+    d2h = out.numel() * 8
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # ---------------- accuracy vs the plain complex128 plan ----------------
+    split_img = out.clone()
+    plan.execute(A, O, Wt, out=split_img)
+    fp64_value = fp64_err = None
+    fp64_ms = None
+    if args.fp64_steps > 0 and args.precision != 'fp64':
+        plan64 = broadband.make_plan(geo, batch=B, precision='fp64')
+        ref = torch.empty_like(out)
+        plan64.execute(A, O, Wt, out=ref)          # warm-up and reference
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.fp64_steps):
+            plan64.execute(A, O, Wt, out=ref, check=False)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fp64_ms = f0.elapsed_time(f1) / args.fp64_steps
+        fp64_value = B / (fp64_ms / 1e3)
+        fp64_err = float(((split_img - ref).abs().amax() / ref.abs().amax()).item())
+        del plan64
+
+    # ---------------- roofline of the dominant kernel ----------------------
+    m, n = geo.fslice[2], geo.fslice[3]
+    M, N = geo.window_shape
+    flops_stage1 = 8.0 * M * m * n * L * B       # complex MACs x 8 (algorithmic)
+    flops_stage2 = 8.0 * M * n * N * L * B
+    mft_ms = kms[1] + kms[2]
+    launches = kcnt[1] + kcnt[2]
+    pk, pk_kind = peaks()
+    peak = pk.get('bf16_tflops_sustained', pk.get('bf16_tflops'))
+    achieved = (flops_stage1 + flops_stage2) * args.steps / (mft_ms / 1e3) / 1e12
+    tr = traffic_per_launch()
+    roofline = {'bound': 'tensor', 'kernel': 'split_mft_kernel (tcgen05, both MFT stages)',
+                'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s', 'frac': achieved / peak,
+                'peak_kind': f'{pk_kind} bf16 dense, sustained',
+                'issued_tflops': 3 * achieved,
+                'traffic': tr.get('traffic_bytes_per_launch') if tr else None,
+                'traffic_note': tr.get('note') if tr else 'no ncu capture committed',
+                'launches': launches, 'avg_launch_ms': mft_ms / max(1, launches),
+                'algorithmic_flops_per_step': flops_stage1 + flops_stage2,
+                'kernel_ms_per_step': {name: kms[i] / args.steps
+                                       for i, name in enumerate(_lib.PROFILE_SLOTS)}}
+
+    # ---------------- CPU baseline (bounded sample) -------------------------
+    cpu_s, idx = cpu_reference(wl, max(1, args.cpu_lambdas), opd[0])
+    cpu_value = 1.0 / (cpu_s * len(wl.wavelengths))
+
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': total_ms / args.steps, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None,
+        'dtype': {'split-fp16': 'fp16 hi+lo split operands, fp32 accumulate',
+                  'split-bf16': 'bf16 hi+lo split operands, fp32 accumulate',
+                  'fp64': 'f64 (complex128)'}[args.precision],
+        'data': 'synthetic (seeded)',
+        'config': config_dict(wl, args, {'precision': args.precision,
+                                         'field': [m, n], 'window': [M, N],
+                                         'parallelism': f'replicas x{world}'}),
+        'p50_ms': statistics.median(step_ms), 'p99_ms': float(np.percentile(step_ms, 99)),
+        'plan_build_ms': plan_ms,
+        'err_vs_fp64': fp64_err,
+        'fp64_plain': None if fp64_value is None else {'value': fp64_value, 'unit': UNIT,
+                                                       'ms_per_psf': fp64_ms / B,
+                                                       'speedup_split_over_fp64': value / world / fp64_value},
+        'roofline': roofline,
+        'cpu_baseline': {'value': cpu_value, 'unit': UNIT, 'cores': os.cpu_count(), 'kind': 'port',
+                         'sample': f'{len(idx)} of {len(wl.wavelengths)} wavelengths of one PSF '
+                                   'through lentil\'s per-segment user loop (numpy restatement '
+                                   'under oracle/), extrapolated linearly'},
+        'e2e': {'value': e2e_value, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
+                'd2h_bytes_per_step': d2h},
+        'gpu_launches': 5 * args.steps,
+        'clocks': clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == '__main__':
+    main()

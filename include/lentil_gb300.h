@@ -1,0 +1,184 @@
+/*
+ * lentil_gb300 — C ABI of the GB300 (sm_103a) far-field diffraction path.
+ *
+ * Each entry point replaces one function of lentil 0.8.8's matrix-Fourier-
+ * transform path (cited beside it).  All pointers are device pointers unless
+ * the comment says "host"; arrays are C-ordered (row-major) and complex
+ * values are interleaved (re, im) doubles, the memory layout of numpy's
+ * complex128.  Every call is asynchronous on the given CUDA stream
+ * (cudaStream_t passed as void*), returns LGB_OK (0) or an error code, and
+ * never aborts the process; lgb_last_error() returns the message of the
+ * calling thread's last failure.
+ *
+ * Precision: LGB_FP64 computes in complex128 (the plain form, parity with
+ * lentil within 1e-12 peak-normalised).  LGB_SPLIT_BF16 / LGB_SPLIT_FP16 run
+ * the contractions on the tcgen05 tensor cores with each operand split into
+ * two 16-bit floats (hi + lo; three partial products, FP32 accumulation).
+ */
+#ifndef LENTIL_GB300_H
+#define LENTIL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; the Python layer maps them to lentil's exception types */
+#define LGB_OK 0
+#define LGB_EINVAL 1        /* ValueError */
+#define LGB_ETYPE 2         /* TypeError */
+#define LGB_ECUDA 3         /* RuntimeError: a CUDA runtime call failed */
+#define LGB_EUNSUPPORTED 4  /* NotImplementedError */
+#define LGB_ETIMEOUT 5      /* a device-side wait hit its time bound */
+#define LGB_EWORKSPACE 6    /* workspace pointer/size too small */
+
+#define LGB_FP64 0
+#define LGB_SPLIT_BF16 1
+#define LGB_SPLIT_FP16 2
+
+typedef struct { double re, im; } lgb_c128; /* == numpy complex128 */
+typedef void* lgb_stream;                   /* == cudaStream_t */
+
+/* Message of this thread's last failed call ("" if none). */
+const char* lgb_last_error(void);
+/* ABI version, (major << 16) | minor. */
+int lgb_version(void);
+
+/* ------------------------------------------------------------------------
+ * DFT matrices.  Replaces lentil/fourier.py:106-110 (_dft2_matrices, with
+ * the centred coordinates of _dft2_coords, lentil/fourier.py:113-121):
+ *   E1[u, r] = exp(-2 pi i alpha_r (R_r + offset_r)(U_u - shift_r))  (M x m)
+ *   E2[s, v] = exp(-2 pi i alpha_c (S_s + offset_c)(V_v - shift_c))  (n x N)
+ * The phase is reduced modulo one cycle in exact fixed point before the
+ * FP64 sincospi.
+ * ---------------------------------------------------------------------- */
+int lgb_dft2_matrices(int m, int n, int M, int N, double alpha_r, double alpha_c,
+                      double shift_r, double shift_c, double offset_r, double offset_c,
+                      lgb_c128* E1, lgb_c128* E2, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Matrix triple product DFT.  Replaces lentil/fourier.py:5-103 (dft2):
+ *   F = E1 . f . E2, times sqrt(|alpha_r alpha_c|) when unitary != 0.
+ * f is m x n, F is M x N (F may not alias f).  The workspace must hold
+ * lgb_dft2_workspace_size(m, n, M, N, precision) bytes, 256-byte aligned.
+ * ---------------------------------------------------------------------- */
+size_t lgb_dft2_workspace_size(int m, int n, int M, int N, int precision);
+int lgb_dft2(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int N,
+             double alpha_r, double alpha_c, double shift_r, double shift_c,
+             double offset_r, double offset_c, int unitary, int precision,
+             void* workspace, size_t workspace_bytes, lgb_stream stream);
+/* Device-side status of the last dft2/idft2 run on this workspace; waits
+ * for the stream.  LGB_ETIMEOUT if a tensor-core pipeline wait expired. */
+int lgb_dft2_status(void* workspace, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Inverse MFT.  Replaces lentil/fourier.py:124-198 (idft2):
+ *   f = conj(dft2(conj(F), alpha, shape, shift, unitary)) / F.size
+ * F is m x n, f is M x N.  Workspace: lgb_idft2_workspace_size bytes.
+ * ---------------------------------------------------------------------- */
+size_t lgb_idft2_workspace_size(int m, int n, int M, int N, int precision);
+int lgb_idft2(const lgb_c128* F, int m, int n, lgb_c128* f, int M, int N,
+              double alpha_r, double alpha_c, double shift_r, double shift_c,
+              int unitary, int precision, void* workspace, size_t workspace_bytes,
+              lgb_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Plane phasor.  Replaces the per-slice phasor of Plane.__mul__,
+ * lentil/plane.py:502-507:
+ *   out[i, j] = amp[r0+i, c0+j] * mask[r0+i, c0+j]
+ *               * exp(2 pi i opd[r0+i, c0+j] / wavelength),   i < m, j < n
+ * amp, mask, opd are H x W float64; a NULL amp / opd means the scalar
+ * amp_value / opd_value (lentil's size-1 planes); a NULL mask means 1.
+ * ---------------------------------------------------------------------- */
+int lgb_phasor(const double* amp, double amp_value, const double* mask,
+               const double* opd, double opd_value, int H, int W,
+               int r0, int c0, int m, int n, double wavelength,
+               lgb_c128* out, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Field overlap-add.  Replaces lentil/field.py:231-305 (insert): the
+ * fm x fn field whose centre sits at offset (off_r, off_c) from the centre
+ * of the om x on output is added, clipped to the output, as
+ *   intensity == 0 :  out += weight * f              (out complex128)
+ *   intensity != 0 :  out += weight * |f|^2          (out float64)
+ * ---------------------------------------------------------------------- */
+int lgb_field_insert(const lgb_c128* f, int fm, int fn, int64_t off_r, int64_t off_c,
+                     void* out, int om, int on, double weight, int intensity,
+                     lgb_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Field product over an intersection.  Replaces the data product of
+ * Field._mul_array, lentil/field.py:130-147 (slices from the host-side
+ * extent algebra of lentil/extent.py:127-150):
+ *   out[i, j] = a[ar0+i, ac0+j] * b[br0+i, bc0+j],  i < om, j < on
+ * A size-1 operand (lentil's broadcast, lentil/field.py:464-484) is passed
+ * with lda == 0 (its single element is used everywhere).
+ * ---------------------------------------------------------------------- */
+int lgb_field_multiply(const lgb_c128* a, int lda, int ar0, int ac0,
+                       const lgb_c128* b, int ldb, int br0, int bc0,
+                       lgb_c128* out, int om, int on, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Broadband PSF plan: the documented user loop
+ *   for lam, w: img = propagate_dft(Wavefront(lam) * pupil, ...).insert(img, w)
+ * (docs/user/performance.rst:44-49) fused for a batch of PSFs that share the
+ * optics: phasor (lentil/plane.py:502-507), propagate_dft's MFT into its
+ * output window (lentil/propagate.py:345-440 with lentil/fourier.py:5-103),
+ * and the weighted |E|^2 overlap-add of Wavefront.insert
+ * (lentil/wavefront.py:145-165, lentil/field.py:231-305).
+ *
+ * A plan owns device memory: the DFT matrices of every wavelength (built at
+ * creation, resident until destroyed) and the per-execute intermediates for
+ * `batch` PSFs.  One field per PSF: the pupil slice rows [r0, r0+m), cols
+ * [c0, c0+n) with lentil's slice offset; all wavelengths land in the same
+ * M x N window at (win_r0, win_c0) of the out_rows x out_cols image.
+ * ---------------------------------------------------------------------- */
+typedef struct lgb_psf_plan_s* lgb_psf_plan;
+
+typedef struct {
+  int H, W;                   /* pupil plane shape */
+  int r0, c0, m, n;           /* field slice of the pupil plane */
+  double offset_r, offset_c;  /* field offset from the plane centre */
+  int M, N;                   /* MFT output window shape */
+  int out_rows, out_cols;     /* output image shape */
+  int win_r0, win_c0;         /* window's first row/col inside the image */
+  int n_wavelengths;          /* L */
+  const double* wavelengths;  /* host [L], metres */
+  const double* alpha_r;      /* host [L], lentil/propagate.py:121-123 */
+  const double* alpha_c;      /* host [L] */
+  const double* shift_r;      /* host [L], output-pixel shift of the DC */
+  const double* shift_c;      /* host [L] */
+  int batch;                  /* PSFs per execute */
+  int precision;              /* LGB_FP64 / LGB_SPLIT_BF16 / LGB_SPLIT_FP16 */
+} lgb_psf_desc;
+
+int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan, lgb_stream stream);
+/* device bytes held by the plan */
+size_t lgb_psf_plan_bytes(lgb_psf_plan plan);
+/* amp, opd: [batch][H][W] float64 (amp already multiplied by the mask);
+ * weights: [batch][L] float64; out: [batch][out_rows][out_cols] float64.
+ * out is overwritten (accumulate == 0) or added to (accumulate != 0). */
+int lgb_psf_execute(lgb_psf_plan plan, const double* amp, const double* opd,
+                    const double* weights, double* out, int accumulate, lgb_stream stream);
+/* Device-side status of the plan's last execute; waits for the stream. */
+int lgb_psf_plan_status(lgb_psf_plan plan, lgb_stream stream);
+/* Optional per-kernel timing of lgb_psf_execute: while enabled, each launch
+ * is bracketed by CUDA events on the execute stream; lgb_psf_plan_kernel_times
+ * waits for them and returns (and resets) the summed milliseconds and launch
+ * counts per slot: phasor, stage-1 MFT, stage-2 MFT, other. */
+#define LGB_PROFILE_PHASOR 0
+#define LGB_PROFILE_MFT1 1
+#define LGB_PROFILE_MFT2 2
+#define LGB_PROFILE_OTHER 3
+#define LGB_PROFILE_SLOTS 4
+int lgb_psf_plan_profile(lgb_psf_plan plan, int enable);
+int lgb_psf_plan_kernel_times(lgb_psf_plan plan, double* ms, int* launches, int n);
+int lgb_psf_plan_destroy(lgb_psf_plan plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LENTIL_GB300_H */

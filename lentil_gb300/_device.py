@@ -1,0 +1,51 @@
+"""Device plumbing: torch supplies device memory and the current stream; all
+arithmetic of the path runs in the library's own kernels."""
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def device():
+    if not torch.cuda.is_available():
+        raise RuntimeError('lentil_gb300 needs a CUDA device (GB300, sm_103a); none is available')
+    _lib.load()
+    return torch.device('cuda', torch.cuda.current_device())
+
+
+def stream_ptr():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def is_tensor(x):
+    return isinstance(x, torch.Tensor)
+
+
+def to_device(x, dtype):
+    """numpy / scalar / tensor -> contiguous CUDA tensor of ``dtype`` (one copy at most)."""
+    dev = device()
+    if is_tensor(x):
+        t = x.to(device=dev, dtype=dtype)
+    else:
+        a = np.asarray(x)
+        if dtype == torch.complex128:
+            a = a.astype(np.complex128, copy=False)
+        elif dtype == torch.float64:
+            a = a.astype(np.float64, copy=False)
+        # np.ascontiguousarray would turn a 0-d array into shape (1,)
+        a = a if a.flags.c_contiguous else a.copy(order='C')
+        t = torch.from_numpy(a).to(device=dev, dtype=dtype)
+    return t.contiguous()
+
+
+def ptr(t):
+    return t.data_ptr() if t is not None else None
+
+
+def workspace(nbytes):
+    """256-byte-aligned device workspace (the caching allocator aligns to 512)."""
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device())
+
+
+def to_host(t):
+    return t.detach().cpu().numpy()

@@ -1,0 +1,122 @@
+"""ctypes binding of ``liblentil_gb300.so`` (declared in include/lentil_gb300.h).
+
+The library is built in-tree by ``lentil_gb300._build``.  There is no CPU
+fallback: every entry of the diffraction path goes through this library and
+raises if it cannot be loaded or no CUDA device is present.
+"""
+import ctypes
+import os
+import threading
+
+from . import _build
+
+OK, EINVAL, ETYPE, ECUDA, EUNSUPPORTED, ETIMEOUT, EWORKSPACE = range(7)
+FP64, SPLIT_BF16, SPLIT_FP16 = 0, 1, 2
+
+PRECISIONS = {'fp64': FP64, 'split-bf16': SPLIT_BF16, 'split-fp16': SPLIT_FP16,
+              'split': SPLIT_FP16}
+
+c_int, c_double, c_size_t, c_void_p = ctypes.c_int, ctypes.c_double, ctypes.c_size_t, ctypes.c_void_p
+c_int64 = ctypes.c_int64
+
+
+class PsfDesc(ctypes.Structure):
+    """Mirror of ``lgb_psf_desc``."""
+    _fields_ = [('H', c_int), ('W', c_int), ('r0', c_int), ('c0', c_int), ('m', c_int), ('n', c_int),
+                ('offset_r', c_double), ('offset_c', c_double), ('M', c_int), ('N', c_int),
+                ('out_rows', c_int), ('out_cols', c_int), ('win_r0', c_int), ('win_c0', c_int),
+                ('n_wavelengths', c_int), ('wavelengths', c_void_p), ('alpha_r', c_void_p),
+                ('alpha_c', c_void_p), ('shift_r', c_void_p), ('shift_c', c_void_p),
+                ('batch', c_int), ('precision', c_int)]
+
+
+# name -> (restype, argtypes); every symbol of include/lentil_gb300.h
+SIGNATURES = {
+    'lgb_last_error': (ctypes.c_char_p, []),
+    'lgb_version': (c_int, []),
+    'lgb_dft2_matrices': (c_int, [c_int, c_int, c_int, c_int, c_double, c_double, c_double,
+                                  c_double, c_double, c_double, c_void_p, c_void_p, c_void_p]),
+    'lgb_dft2_workspace_size': (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
+    'lgb_dft2': (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double, c_double,
+                         c_double, c_double, c_double, c_double, c_int, c_int, c_void_p, c_size_t,
+                         c_void_p]),
+    'lgb_dft2_status': (c_int, [c_void_p, c_void_p]),
+    'lgb_idft2_workspace_size': (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
+    'lgb_idft2': (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double, c_double,
+                          c_double, c_double, c_int, c_int, c_void_p, c_size_t, c_void_p]),
+    'lgb_phasor': (c_int, [c_void_p, c_double, c_void_p, c_void_p, c_double, c_int, c_int, c_int,
+                           c_int, c_int, c_int, c_double, c_void_p, c_void_p]),
+    'lgb_field_insert': (c_int, [c_void_p, c_int, c_int, c_int64, c_int64, c_void_p, c_int, c_int,
+                                 c_double, c_int, c_void_p]),
+    'lgb_field_multiply': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int, c_int,
+                                   c_void_p, c_int, c_int, c_void_p]),
+    'lgb_psf_plan_create': (c_int, [ctypes.POINTER(PsfDesc), ctypes.POINTER(c_void_p), c_void_p]),
+    'lgb_psf_plan_bytes': (c_size_t, [c_void_p]),
+    'lgb_psf_execute': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    'lgb_psf_plan_status': (c_int, [c_void_p, c_void_p]),
+    'lgb_psf_plan_destroy': (c_int, [c_void_p]),
+    'lgb_psf_plan_profile': (c_int, [c_void_p, c_int]),
+    'lgb_psf_plan_kernel_times': (c_int, [c_void_p, ctypes.POINTER(c_double),
+                                          ctypes.POINTER(c_int), c_int]),
+}
+PROFILE_SLOTS = ('phasor', 'mft_stage1', 'mft_stage2', 'other')
+
+_lock = threading.Lock()
+_lib = None
+
+
+class LentilGpuError(RuntimeError):
+    """A CUDA failure inside the library."""
+
+
+class DeviceTimeout(LentilGpuError):
+    """A bounded device-side wait expired; the results of the call are invalid."""
+
+
+_EXC = {EINVAL: ValueError, ETYPE: TypeError, ECUDA: LentilGpuError,
+        EUNSUPPORTED: NotImplementedError, ETIMEOUT: DeviceTimeout, EWORKSPACE: ValueError}
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load (building first if needed) the CUDA library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_missing and not _build.up_to_date():
+            _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(f'lentil_gb300 CUDA library missing: {path}')
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(status):
+    """Raise the exception lentil raises for the same condition."""
+    if status == OK:
+        return
+    msg = load().lgb_last_error().decode(errors='replace')
+    raise _EXC.get(status, LentilGpuError)(msg)
+
+
+def call(name, *args):
+    check(getattr(load(), name)(*args))
+
+
+def precision_code(precision):
+    try:
+        return PRECISIONS[precision]
+    except KeyError:
+        raise ValueError(f"unknown precision {precision!r}; expected one of {sorted(PRECISIONS)}")

@@ -1,0 +1,267 @@
+"""Fused broadband PSFs: lentil's documented user loop
+
+    for lam, w in zip(wavelengths, weights):
+        img = propagate_dft(Wavefront(lam) * pupil, pixelscale, ...).insert(img, w)
+
+(docs/user/performance.rst:44-49) as one plan execution on the GPU for a
+batch of PSFs that share optics.  The plan keeps the DFT matrices of every
+wavelength resident, builds the phasor of every (PSF, wavelength) straight
+into the tensor-core operand layout, and accumulates w * |E|^2 in the MFT
+epilogue.
+
+Fields that share one window and one shift per wavelength are summed before
+the transform (the MFT is linear and lentil's ``Wavefront.intensity`` sums
+overlapping fields coherently), so a segmented pupil without per-segment
+tilts is one dense field.  Pupils whose segments carry their own tilts are
+propagated field by field through ``propagate_dft`` (same kernels, one
+launch sequence per field) and overlap-added on the device.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _device as dv
+from . import _lib
+from . import util
+from .propagate import plan_fields
+
+
+class _ProbeField:
+    """Geometry-only stand-in for a Field (offset, shape, tilts)."""
+
+    def __init__(self, offset, shape, tilt):
+        self.offset, self.shape, self.tilt = offset, shape, tilt
+
+    shift = None  # bound below
+
+
+def _probe_shift(self, z, wavelength, pixelscale, oversample, indexing='ij'):
+    from .field import Field
+    return Field.shift(self, z, wavelength, pixelscale, oversample, indexing)
+
+
+_ProbeField.shift = _probe_shift
+
+
+class _ProbeWavefront:
+    def __init__(self, wavelength, pixelscale, focal_length, shape, data, ptype):
+        self.wavelength, self.pixelscale, self.focal_length = wavelength, pixelscale, focal_length
+        self.shape, self.data, self.ptype = shape, data, ptype
+
+
+class PSFPlan:
+    """Device plan for a batch of broadband PSFs with fixed optics.
+
+    Parameters mirror the user loop: pupil-plane shape and field slice, the
+    wavelengths, per-wavelength MFT sampling ``alpha`` and output shift, the
+    MFT window inside the output image, the batch size and the precision."""
+
+    def __init__(self, plane_shape, field_slice, field_offset, wavelengths, alphas, shifts,
+                 window_shape, image_shape, window_origin, batch=1, precision='split'):
+        lib = _lib.load()
+        dv.device()
+        self.plane_shape = tuple(int(x) for x in plane_shape)
+        self.field_slice = tuple(int(x) for x in field_slice)
+        self.image_shape = tuple(int(x) for x in image_shape)
+        self.wavelengths = np.ascontiguousarray(wavelengths, dtype=np.float64)
+        self.L = len(self.wavelengths)
+        self.batch = int(batch)
+        self.precision = precision
+        ar = np.ascontiguousarray([a[0] for a in alphas], dtype=np.float64)
+        ac = np.ascontiguousarray([a[1] for a in alphas], dtype=np.float64)
+        sr = np.ascontiguousarray([s[0] for s in shifts], dtype=np.float64)
+        sc = np.ascontiguousarray([s[1] for s in shifts], dtype=np.float64)
+        r0, c0, m, n = self.field_slice
+        d = _lib.PsfDesc()
+        d.H, d.W = self.plane_shape
+        d.r0, d.c0, d.m, d.n = r0, c0, m, n
+        d.offset_r, d.offset_c = float(field_offset[0]), float(field_offset[1])
+        d.M, d.N = int(window_shape[0]), int(window_shape[1])
+        d.out_rows, d.out_cols = self.image_shape
+        d.win_r0, d.win_c0 = int(window_origin[0]), int(window_origin[1])
+        d.n_wavelengths = self.L
+        keep = (self.wavelengths, ar, ac, sr, sc)
+        d.wavelengths, d.alpha_r, d.alpha_c, d.shift_r, d.shift_c = [a.ctypes.data for a in keep]
+        d.batch = self.batch
+        d.precision = _lib.precision_code(precision)
+        self.desc = d
+        h = ctypes.c_void_p()
+        _lib.check(lib.lgb_psf_plan_create(ctypes.byref(d), ctypes.byref(h), dv.stream_ptr()))
+        self._h = h
+        self.nbytes = lib.lgb_psf_plan_bytes(h)
+
+    def __del__(self):
+        h = getattr(self, '_h', None)
+        if h is not None and h.value:
+            try:
+                _lib.load().lgb_psf_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def execute(self, amp, opd, weights, out=None, accumulate=False, check=True):
+        """amp (mask applied), opd: [batch, H, W] float64 CUDA tensors;
+        weights: [batch, L]; returns out [batch, rows, cols] float64."""
+        dev = dv.device()
+        amp = amp if amp.dtype == torch.float64 and amp.is_contiguous() else amp.double().contiguous()
+        opd = opd if opd.dtype == torch.float64 and opd.is_contiguous() else opd.double().contiguous()
+        weights = dv.to_device(weights, torch.float64)
+        shp = (self.batch,) + self.plane_shape
+        if tuple(amp.shape) != shp or tuple(opd.shape) != shp:
+            raise ValueError(f'amp/opd must have shape {shp}')
+        if weights.numel() != self.batch * self.L:
+            raise ValueError(f'weights must have {self.batch * self.L} entries')
+        if out is None:
+            out = torch.empty((self.batch,) + self.image_shape, dtype=torch.float64, device=dev)
+            accumulate = False
+        _lib.call('lgb_psf_execute', self._h, amp.data_ptr(), opd.data_ptr(), weights.data_ptr(),
+                  out.data_ptr(), int(bool(accumulate)), dv.stream_ptr())
+        if check:
+            _lib.call('lgb_psf_plan_status', self._h, dv.stream_ptr())
+        return out
+
+
+def dense_field(pupil):
+    """Merged single field of a pupil without per-segment tilts: the slice
+    covering every segment and amp*sum(masks) over it (lentil/plane.py:494-514
+    summed over segments).  Returns (slice, amp_eff, opd) on the host."""
+    amp = np.asarray(dv.to_host(pupil.amplitude) if dv.is_tensor(pupil.amplitude) else pupil.amplitude,
+                     dtype=float)
+    opd = np.asarray(dv.to_host(pupil.opd) if dv.is_tensor(pupil.opd) else pupil.opd, dtype=float)
+    mask = pupil.mask
+    mask = np.asarray(dv.to_host(mask) if dv.is_tensor(mask) else mask, dtype=float)
+    if amp.ndim != 2:
+        raise NotImplementedError('broadband plan needs an amplitude array')
+    gmask = mask if mask.ndim == 2 else mask.sum(axis=0)
+    if mask.ndim == 2:
+        s = util.boundary_slice(mask)
+    else:
+        sl = [util.boundary_slice(x) for x in mask]
+        s = np.s_[min(x[0].start for x in sl):max(x[0].stop for x in sl),
+                  min(x[1].start for x in sl):max(x[1].stop for x in sl)]
+    opd_full = np.broadcast_to(opd, amp.shape) if opd.size == 1 else opd
+    return s, amp * gmask, np.ascontiguousarray(opd_full, dtype=float)
+
+
+def broadband_psf(pupil, wavelengths, weights, pixelscale, shape=None, prop_shape=None,
+                  oversample=2, mask=None, precision='split', out=None):
+    """Sum over wavelengths of weight * propagate_dft(Wavefront(lam) * pupil).intensity.
+
+    Equivalent to lentil's broadband loop; returns a float64 image (numpy, or
+    a CUDA tensor when the pupil holds tensors).  ``out`` (optional) is added
+    to, as ``Wavefront.insert`` does."""
+    from .wavefront import Wavefront
+    from . import propagate as prop
+    wavelengths = np.atleast_1d(np.asarray(wavelengths, dtype=float))
+    weights = np.atleast_1d(np.asarray(weights, dtype=float))
+    tensor_io = pupil._tensor_io() if hasattr(pupil, '_tensor_io') else False
+    if len(pupil.tilt) > 1:
+        # per-segment tilts: every segment is its own field with its own window
+        img = None
+        dev_out = None if out is None else dv.to_device(out, torch.float64)
+        for lam, w in zip(wavelengths, weights):
+            wf = prop.propagate_dft(Wavefront(lam) * pupil, pixelscale, shape=shape,
+                                    prop_shape=prop_shape, oversample=oversample, mask=mask,
+                                    precision=precision)
+            if dev_out is None:
+                dev_out = torch.zeros(tuple(int(s) for s in wf.shape), dtype=torch.float64,
+                                      device=dv.device())
+            dev_out = wf.insert(dev_out, weight=w)
+        img = dev_out
+        return _deliver(img, out, tensor_io)
+
+    s, amp_eff, opd = dense_field(pupil)
+    plane_shape = amp_eff.shape
+    geo = plan_geometry(plane_shape, s, list(pupil.tilt), pupil.pixelscale, pupil.focal_length,
+                        pupil.ptype, wavelengths, pixelscale, shape, prop_shape, oversample, mask)
+    dev = dv.device()
+    img = torch.zeros(geo.shape_out, dtype=torch.float64, device=dev) if out is None else \
+        dv.to_device(out, torch.float64)
+    if not geo.keep:
+        return _deliver(img, out, tensor_io)
+    plan = _cached_plan(geo, precision)
+    a = dv.to_device(amp_eff, torch.float64).reshape((1,) + plane_shape)
+    o = dv.to_device(opd, torch.float64).reshape((1,) + plane_shape)
+    w = dv.to_device(weights[geo.keep], torch.float64).reshape(1, -1)
+    plan.execute(a, o, w, out=img.reshape((1,) + geo.shape_out), accumulate=True)
+    return _deliver(img, out, tensor_io)
+
+
+class Geometry:
+    """Where one merged field lands for every wavelength of a broadband PSF."""
+    __slots__ = ('plane_shape', 'fslice', 'offset', 'wavelengths', 'alphas', 'shifts',
+                 'window_shape', 'window_origin', 'shape_out', 'keep')
+
+
+def plan_geometry(plane_shape, s, tilts, dx, focal_length, ptype, wavelengths, du, shape=None,
+                  prop_shape=None, oversample=2, mask=None):
+    """Window maths of propagate_dft (lentil/propagate.py:373-438) for one
+    field slice ``s`` of the pupil plane and every wavelength; wavelengths
+    whose window misses the output are dropped (``keep`` lists the rest)."""
+    off = util.slice_offset(s, plane_shape)
+    r0, c0 = int(s[0].start), int(s[1].start)
+    m, n = int(s[0].stop) - r0, int(s[1].stop) - c0
+    g = Geometry()
+    g.plane_shape, g.fslice, g.offset = tuple(plane_shape), (r0, c0, m, n), off
+    g.alphas, g.shifts, g.keep = [], [], []
+    window, shape_out = None, None
+    for i, lam in enumerate(np.atleast_1d(wavelengths)):
+        probe = _ProbeWavefront(lam, dx, focal_length, plane_shape,
+                                [_ProbeField(off, (m, n), list(tilts))], ptype)
+        _, shape_out, _, jobs = plan_fields(probe, du, shape, prop_shape, oversample, mask)
+        if not jobs:
+            continue
+        j = jobs[0]
+        win = (tuple(int(x) for x in j.shape), tuple(int(x) for x in j.offset_out))
+        if window is not None and win != window:
+            raise NotImplementedError('wavelength-dependent output windows are not fused')
+        window = win
+        g.keep.append(i)
+        g.alphas.append(tuple(float(a) for a in j.alpha))
+        g.shifts.append(tuple(float(x) for x in j.shift))
+    g.shape_out = tuple(int(x) for x in shape_out)
+    g.wavelengths = np.atleast_1d(np.asarray(wavelengths, dtype=float))[g.keep]
+    if window is not None:
+        wshape, woff = window
+        # window origin inside the image: the placement rule of lentil/field.py:267
+        g.window_shape = wshape
+        g.window_origin = (g.shape_out[0] // 2 - wshape[0] // 2 + woff[0],
+                           g.shape_out[1] // 2 - wshape[1] // 2 + woff[1])
+    else:
+        g.window_shape = g.window_origin = None
+    return g
+
+
+def make_plan(geo, batch=1, precision='split'):
+    """PSFPlan for a Geometry."""
+    return PSFPlan(geo.plane_shape, geo.fslice, geo.offset, geo.wavelengths, geo.alphas, geo.shifts,
+                   geo.window_shape, geo.shape_out, geo.window_origin, batch=batch,
+                   precision=precision)
+
+
+def _deliver(img, out, tensor_io):
+    if out is not None and not dv.is_tensor(out):
+        out[...] = dv.to_host(img)
+        return out
+    if out is not None:
+        if img.data_ptr() != out.data_ptr():
+            out.copy_(img)
+        return out
+    return img if tensor_io else dv.to_host(img)
+
+
+_PLANS = {}
+
+
+def _cached_plan(geo, precision, batch=1):
+    key = (geo.plane_shape, geo.fslice, tuple(geo.offset), tuple(geo.wavelengths.tolist()),
+           tuple(geo.alphas), tuple(geo.shifts), geo.window_shape, geo.shape_out,
+           geo.window_origin, precision, batch)
+    p = _PLANS.get(key)
+    if p is None:
+        if len(_PLANS) >= 8:
+            _PLANS.pop(next(iter(_PLANS)))
+        p = make_plan(geo, batch=batch, precision=precision)
+        _PLANS[key] = p
+    return p

@@ -1,0 +1,348 @@
+// HBM-bound elementwise kernels of the diffraction path:
+//   K2  phasor amp*mask*exp(2 pi i opd / lambda)  (lentil/plane.py:502-507)
+//   K2s the same phasor written straight into the split 16-bit, transposed
+//       operand of the tensor-core MFT, for every wavelength of a batch
+//   K5  clipped field overlap-add / |E|^2 insert  (lentil/field.py:231-305)
+//       and the intersection product of Field.__mul__ (lentil/field.py:130-147)
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace lgb {
+
+// ---------------------------------------------------------------------------
+// K2: complex128 phasor over one slice
+// ---------------------------------------------------------------------------
+__global__ void phasor_c128_kernel(const double* __restrict__ amp, double amp_value,
+                                   const double* __restrict__ mask,
+                                   const double* __restrict__ opd, double opd_value, int W,
+                                   int r0, int c0, int m, int n, double two_over_lambda,
+                                   double2* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= n || i >= m) return;
+  const size_t p = (size_t)(r0 + i) * W + (c0 + j);
+  double a = amp ? amp[p] : amp_value;
+  if (mask) a *= mask[p];
+  const double o = opd ? opd[p] : opd_value;
+  double s, c;
+  sincospi(o * two_over_lambda, &s, &c);     // exp(+2 pi i opd/lambda)
+  out[(size_t)i * n + j] = make_double2(a * c, a * s);
+}
+
+__global__ void phasor_batch_c128_kernel(const double* __restrict__ amp,
+                                         const double* __restrict__ opd, int H, int W, int r0,
+                                         int c0, int m, int n,
+                                         const double* __restrict__ two_over_lambda, int L,
+                                         double2* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  const int b = blockIdx.z;
+  if (j >= n || i >= m) return;
+  const size_t p = ((size_t)b * H + r0 + i) * W + (c0 + j);
+  const double a = amp[p], o = opd[p];
+  for (int l = 0; l < L; ++l) {
+    double s, c;
+    sincospi(o * two_over_lambda[l], &s, &c);
+    out[(((size_t)b * L + l) * m + i) * n + j] = make_double2(a * c, a * s);
+  }
+}
+
+int launch_phasor_batch_c128(const double* amp, const double* opd, int H, int W, int r0, int c0,
+                             int m, int n, const double* two_over_lambda, int L, int batch,
+                             double2* out, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return LGB_OK;
+  dim3 grid(cdiv(n, 128), m, batch);
+  phasor_batch_c128_kernel<<<grid, 128, 0, s>>>(amp, opd, H, W, r0, c0, m, n, two_over_lambda,
+                                                L, out);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// K2s: split 16-bit transposed field operand.
+// Output row c (field column), K index r (field row) for the real part and
+// kp + r for the imaginary part: f^T in the stage-1 B-operand layout.
+// One block = 64 field rows x 32 field columns, looping over wavelengths.
+// ---------------------------------------------------------------------------
+constexpr int TR = 64, TC = 32, TPAD = 8;
+
+template <bool BF16, bool PHASOR>
+__global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a) {
+  __shared__ __align__(16) uint16_t tile[4][TC][TR + TPAD];   // re_hi, re_lo, im_hi, im_lo
+  const int tid = threadIdx.x;
+  const int rt = blockIdx.x * TR, ct = blockIdx.y * TC;
+  const int b = blockIdx.z;                         // PSF
+  const float sf = pow2_scale_for(a.maxabs[b]);
+
+  // load 8 pixels per thread once (coalesced along the field columns)
+  float amp_r[8], o_hi[8], o_lo[8];
+  float2 fv[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int p = tid + 256 * k, rl = p >> 5, cl = p & 31;
+    const int r = rt + rl, c = ct + cl;
+    amp_r[k] = 0.f; o_hi[k] = 0.f; o_lo[k] = 0.f; fv[k] = make_float2(0.f, 0.f);
+    if (r < a.m && c < a.n) {
+      if (PHASOR) {
+        const size_t q = ((size_t)b * a.H + (a.r0 + r)) * a.W + (a.c0 + c);
+        const double o = a.opd[q];
+        amp_r[k] = (float)a.amp[q] * sf;
+        o_hi[k] = (float)o;
+        o_lo[k] = (float)(o - (double)o_hi[k]);
+      } else {
+        const double2 v = a.field[(size_t)r * a.n + c];
+        fv[k] = make_float2((float)v.x * sf, (float)v.y * sf);
+      }
+    }
+  }
+
+  const int L = PHASOR ? a.L : 1;
+  for (int l = 0; l < L; ++l) {
+    if (PHASOR) {
+      const float2 kk = a.khalf[l];                  // 2/lambda as a float-float pair
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        // x = opd * 2/lambda half-cycles, reduced mod 2 before sincospi
+        const float p = o_hi[k] * kk.x;
+        float e = fmaf(o_hi[k], kk.x, -p);
+        e = fmaf(o_hi[k], kk.y, fmaf(o_lo[k], kk.x, e));
+        const float x = (p - 2.f * rintf(0.5f * p)) + e;
+        float sn, cs;
+        sincospif(x, &sn, &cs);
+        fv[k] = make_float2(amp_r[k] * cs, amp_r[k] * sn);
+      }
+    }
+    __syncthreads();   // previous wavelength's tile fully written out
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int p = tid + 256 * k, rl = p >> 5, cl = p & 31;
+      uint16_t h, lo;
+      Split16<BF16>::split(fv[k].x, h, lo);
+      tile[0][cl][rl] = h; tile[1][cl][rl] = lo;
+      Split16<BF16>::split(fv[k].y, h, lo);
+      tile[2][cl][rl] = h; tile[3][cl][rl] = lo;
+    }
+    __syncthreads();
+    const size_t q = (size_t)b * L + l;
+    const size_t K = 2 * (size_t)a.kp;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int v = tid + 256 * k;                   // 1024 16-byte vectors
+      const int plane = v >> 8, cl = (v >> 3) & 31, seg = v & 7;
+      const int c = ct + cl, r = rt + seg * 8;
+      if (c < a.n && r < a.kp) {
+        uint16_t* dst = (plane & 1) ? a.lo : a.hi;
+        const size_t off = (q * a.n + c) * K + ((plane >> 1) ? a.kp : 0) + r;
+        *reinterpret_cast<uint4*>(dst + off) = *reinterpret_cast<const uint4*>(&tile[plane][cl][seg * 8]);
+      }
+    }
+  }
+}
+
+int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
+  dim3 grid(cdiv(a.kp, TR), cdiv(a.n, TC), a.amp ? a.batch : 1);
+  if (a.amp) {
+    if (bf16) split_field_T_kernel<true, true><<<grid, 256, 0, s>>>(a);
+    else split_field_T_kernel<false, true><<<grid, 256, 0, s>>>(a);
+  } else {
+    if (bf16) split_field_T_kernel<true, false><<<grid, 256, 0, s>>>(a);
+    else split_field_T_kernel<false, false><<<grid, 256, 0, s>>>(a);
+  }
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// max |.| reductions feeding the power-of-two split scales
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void maxabs_amp_kernel(const double* __restrict__ amp, int H, int W, int r0, int c0,
+                                  int m, int n, float* __restrict__ out) {
+  const int b = blockIdx.y;
+  float v = 0.f;
+  const size_t total = (size_t)m * n;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < total;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p / n), j = (int)(p % n);
+    v = fmaxf(v, (float)fabs(amp[((size_t)b * H + r0 + i) * W + c0 + j]));
+  }
+  v = warp_max(v);
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(out + b), __float_as_int(v));
+}
+
+__global__ void maxabs_c128_kernel(const double2* __restrict__ f, int count, float* __restrict__ out) {
+  float v = 0.f;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x) {
+    const double2 z = f[p];
+    v = fmaxf(v, fmaxf((float)fabs(z.x), (float)fabs(z.y)));
+  }
+  v = warp_max(v);
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(out), __float_as_int(v));
+}
+
+int launch_maxabs_amp(const double* amp, int batch, int H, int W, int r0, int c0, int m, int n,
+                      float* out, cudaStream_t s) {
+  LGB_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * batch, s));
+  const int blocks = (int)std::min<size_t>(2 * (size_t)sm_count(), cdiv(m * n, 256));
+  maxabs_amp_kernel<<<dim3(blocks > 0 ? blocks : 1, batch), 256, 0, s>>>(amp, H, W, r0, c0, m, n, out);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+int launch_maxabs_c128(const double2* f, int count, float* out, cudaStream_t s) {
+  LGB_CUDA(cudaMemsetAsync(out, 0, sizeof(float), s));
+  const int blocks = std::max(1, std::min(2 * sm_count(), cdiv(count, 256)));
+  maxabs_c128_kernel<<<blocks, 256, 0, s>>>(f, count, out);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 intensity window (reduced into by the tensor-core epilogue) added to
+// the float64 output image
+// ---------------------------------------------------------------------------
+__global__ void window_add_kernel(const float* __restrict__ wbuf, int M, int N, int ldw,
+                                  double* __restrict__ out, int ld_out, long long out_bs,
+                                  int win_r0, int win_c0) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  const int u = blockIdx.y, b = blockIdx.z;
+  if (v >= N || u >= M) return;
+  out[(size_t)b * out_bs + (size_t)(win_r0 + u) * ld_out + win_c0 + v] +=
+      (double)wbuf[((size_t)b * M + u) * ldw + v];
+}
+
+int launch_window_add(const float* wbuf, int M, int N, int ldw, int batch, double* out, int ld_out,
+                      long long out_bs, int win_r0, int win_c0, cudaStream_t s) {
+  if (M <= 0 || N <= 0 || batch <= 0) return LGB_OK;
+  dim3 grid(cdiv(N, 128), M, batch);
+  window_add_kernel<<<grid, 128, 0, s>>>(wbuf, M, N, ldw, out, ld_out, out_bs, win_r0, win_c0);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// conj(in) * scale -> out (idft2 through dft2, lentil/fourier.py:193-198)
+// ---------------------------------------------------------------------------
+__global__ void conj_scale_kernel(const double2* __restrict__ in, double2* __restrict__ out,
+                                  size_t count, double scale) {
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < count;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const double2 z = in[p];
+    out[p] = make_double2(z.x * scale, -z.y * scale);
+  }
+}
+
+int launch_conj_scale(const double2* in, double2* out, size_t count, double scale, cudaStream_t s) {
+  if (count == 0) return LGB_OK;
+  const int blocks = (int)std::min<size_t>(4 * (size_t)sm_count(), (count + 255) / 256);
+  conj_scale_kernel<<<blocks, 256, 0, s>>>(in, out, count, scale);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// K5: clipped overlap-add
+// ---------------------------------------------------------------------------
+template <bool INTENSITY>
+__global__ void insert_kernel(const double2* __restrict__ f, int fn, int fr0, int fc0,
+                              void* __restrict__ out, int on, int or0, int oc0, int rows, int cols,
+                              double weight) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= cols || i >= rows) return;
+  const double2 z = f[(size_t)(fr0 + i) * fn + fc0 + j];
+  const size_t o = (size_t)(or0 + i) * on + oc0 + j;
+  if (INTENSITY) {
+    double* d = static_cast<double*>(out);
+    // lentil: abs(f**2) * weight
+    d[o] += (z.x * z.x + z.y * z.y) * weight;
+  } else {
+    double2* d = static_cast<double2*>(out);
+    double2 t = d[o];
+    t.x += z.x * weight;
+    t.y += z.y * weight;
+    d[o] = t;
+  }
+}
+
+__global__ void multiply_kernel(const double2* __restrict__ a, int lda, int ar0, int ac0,
+                                const double2* __restrict__ b, int ldb, int br0, int bc0,
+                                double2* __restrict__ out, int om, int on) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= on || i >= om) return;
+  const double2 x = lda ? a[(size_t)(ar0 + i) * lda + ac0 + j] : a[0];
+  const double2 y = ldb ? b[(size_t)(br0 + i) * ldb + bc0 + j] : b[0];
+  out[(size_t)i * on + j] = make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+}
+
+}  // namespace lgb
+
+using namespace lgb;
+
+extern "C" int lgb_phasor(const double* amp, double amp_value, const double* mask,
+                          const double* opd, double opd_value, int H, int W, int r0, int c0,
+                          int m, int n, double wavelength, lgb_c128* out, lgb_stream stream) {
+  LGB_REQUIRE(out, LGB_EINVAL, "phasor: null output");
+  LGB_REQUIRE(m >= 0 && n >= 0 && r0 >= 0 && c0 >= 0, LGB_EINVAL, "phasor: negative slice");
+  LGB_REQUIRE((!amp && !mask && !opd) || (r0 + m <= H && c0 + n <= W), LGB_EINVAL,
+              "phasor: slice outside the plane");
+  LGB_REQUIRE(wavelength != 0.0, LGB_EINVAL, "phasor: wavelength must be nonzero");
+  if (m == 0 || n == 0) return LGB_OK;
+  dim3 grid(cdiv(n, 128), m);
+  phasor_c128_kernel<<<grid, 128, 0, as_stream(stream)>>>(amp, amp_value, mask, opd, opd_value,
+                                                          W, r0, c0, m, n, 2.0 / wavelength,
+                                                          reinterpret_cast<double2*>(out));
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+extern "C" int lgb_field_insert(const lgb_c128* f, int fm, int fn, int64_t off_r, int64_t off_c,
+                                void* out, int om, int on, double weight, int intensity,
+                                lgb_stream stream) {
+  LGB_REQUIRE(f && out, LGB_EINVAL, "field_insert: null pointer");
+  LGB_REQUIRE(fm > 0 && fn > 0 && om > 0 && on > 0, LGB_EINVAL, "field_insert: empty array");
+  // lentil/field.py:259-299: upper-left corner of the shifted field in the
+  // output, then clip both index ranges to the output
+  int64_t fr0 = 0, fr1 = fm, fc0 = 0, fc1 = fn;
+  int64_t or0 = om / 2 - fm / 2 + off_r, or1 = or0 + fm;
+  int64_t oc0 = on / 2 - fn / 2 + off_c, oc1 = oc0 + fn;
+  if (or0 < 0) { fr0 = -or0; or0 = 0; }
+  if (or1 > om) { fr1 -= or1 - om; or1 = om; }
+  if (oc0 < 0) { fc0 = -oc0; oc0 = 0; }
+  if (oc1 > on) { fc1 -= oc1 - on; oc1 = on; }
+  const int64_t rows = std::min(fr1 - fr0, or1 - or0), cols = std::min(fc1 - fc0, oc1 - oc0);
+  if (rows <= 0 || cols <= 0) return LGB_OK;   // numpy's empty-slice add is a no-op
+  dim3 grid(cdiv((int)cols, 128), (unsigned)rows);
+  if (intensity)
+    insert_kernel<true><<<grid, 128, 0, as_stream(stream)>>>(
+        reinterpret_cast<const double2*>(f), fn, (int)fr0, (int)fc0, out, on, (int)or0, (int)oc0,
+        (int)rows, (int)cols, weight);
+  else
+    insert_kernel<false><<<grid, 128, 0, as_stream(stream)>>>(
+        reinterpret_cast<const double2*>(f), fn, (int)fr0, (int)fc0, out, on, (int)or0, (int)oc0,
+        (int)rows, (int)cols, weight);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+extern "C" int lgb_field_multiply(const lgb_c128* a, int lda, int ar0, int ac0,
+                                  const lgb_c128* b, int ldb, int br0, int bc0, lgb_c128* out,
+                                  int om, int on, lgb_stream stream) {
+  LGB_REQUIRE(a && b && out, LGB_EINVAL, "field_multiply: null pointer");
+  LGB_REQUIRE(om >= 0 && on >= 0, LGB_EINVAL, "field_multiply: negative shape");
+  if (om == 0 || on == 0) return LGB_OK;
+  dim3 grid(cdiv(on, 128), om);
+  multiply_kernel<<<grid, 128, 0, as_stream(stream)>>>(
+      reinterpret_cast<const double2*>(a), lda, ar0, ac0, reinterpret_cast<const double2*>(b),
+      ldb, br0, bc0, reinterpret_cast<double2*>(out), om, on);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}

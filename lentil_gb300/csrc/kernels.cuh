@@ -1,0 +1,97 @@
+// Launchers shared between the translation units of the library.
+#pragma once
+
+#include "common.cuh"
+
+namespace lgb {
+
+// dft_matrices.cu --------------------------------------------------------
+int launch_dft_matrix_c128(const PhaseAxis& ax, int len_in, int len_out, double2* E,
+                           bool e1_layout, cudaStream_t s);
+int launch_e1_block_split(const PhaseAxis* d_axes, int L, int m, int M, int kp, int rows_padded,
+                          bool bf16, uint16_t* hi, uint16_t* lo, cudaStream_t s);
+int launch_e2_block_split(const PhaseAxis* d_axes, int L, int n, int N, int kp, int rows_padded,
+                          bool bf16, uint16_t* hi, uint16_t* lo, cudaStream_t s);
+
+// elementwise.cu ---------------------------------------------------------
+// per-PSF scale of the field fed to the 16-bit split: 2^-e with
+// max|component| <= 2^e, so every scaled component lies in [-1, 1]
+__device__ __forceinline__ float pow2_scale_for(float maxabs) {
+  if (!(maxabs > 0.f) || !isfinite(maxabs)) return 1.f;
+  int e;
+  frexpf(maxabs, &e);
+  return ldexpf(1.f, -e);
+}
+
+// Input of the split operand builder: either a phasor from amplitude/OPD
+// planes (one per PSF, for a list of wavelengths) or a complex field.
+struct SplitFieldArgs {
+  // phasor mode
+  const double* amp;       // [batch][H][W] (mask already applied)
+  const double* opd;       // [batch][H][W]
+  int H, W, r0, c0;
+  const float2* khalf;     // [L] (hi, lo) float pair of 2/lambda
+  // complex mode
+  const double2* field;    // [m][n] complex128 (batch 1, L 1)
+  // common
+  int m, n, kp, L, batch;
+  const float* maxabs;     // [batch] max |component| of the field (device)
+  uint16_t* hi;            // [batch*L][n][2*kp]
+  uint16_t* lo;
+};
+int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s);
+
+// max over the slice of |amp| (phasor mode) or max(|re|,|im|) (complex mode)
+int launch_maxabs_amp(const double* amp, int batch, int H, int W, int r0, int c0, int m, int n,
+                      float* out, cudaStream_t s);
+int launch_maxabs_c128(const double2* f, int count, float* out, cudaStream_t s);
+
+// out[i,j] (+)= (re, im) scaled; generic complex128 copy/convert kernels
+int launch_conj_scale(const double2* in, double2* out, size_t count, double scale, cudaStream_t s);
+
+// mft_fp64.cu ------------------------------------------------------------
+// C[b] = alpha * A[b] . B[b] (complex128), row-major with leading dims and
+// batch strides (elements).  beta == 0 overwrites C.
+int launch_zgemm(int M, int N, int K, const double2* A, int lda, long long sA,
+                 const double2* B, int ldb, long long sB, double2* C, int ldc, long long sC,
+                 int batch, double alpha, cudaStream_t s);
+// out[b] += sum_l weights[b][l] * unit2[l] * |F[b][l]|^2 into a window (FP64)
+int launch_intensity_accum_c128(const double2* F, int M, int N, long long sF, int batch_inner,
+                                const double* weights, const double* unit2, double* out,
+                                int ld_out, long long s_out, int win_r0, int win_c0, int n_outer,
+                                cudaStream_t s);
+// batched complex128 phasor: out[b*L + l] = amp[b] * exp(2 pi i opd[b] / lambda_l) on a slice
+int launch_phasor_batch_c128(const double* amp, const double* opd, int H, int W, int r0, int c0,
+                             int m, int n, const double* two_over_lambda, int L, int batch,
+                             double2* out, cudaStream_t s);
+
+// mft_split.cu -----------------------------------------------------------
+struct SplitMftProblem {
+  // stage 1: G = E1 . f      A: E1 block [L][mrows1][2*kp1]   B: f^T [Q][n][2*kp1]
+  // stage 2: F = G . E2      A: G        [Q][M][2*kp2]        B: E2 block [L][nrows2][2*kp2]
+  int m, n, M, N;          // field and window shapes
+  int kp1, kp2;            // round_up(m, 32), round_up(n, 32)
+  int L, batch;            // wavelengths, PSFs; Q = batch * L problems
+  bool bf16;
+  const uint16_t *e1_hi, *e1_lo, *f_hi, *f_lo, *e2_hi, *e2_lo;
+  uint16_t *g_hi, *g_lo;   // stage-1 output / stage-2 A operand
+  const float* maxabs;     // [batch], max |component| of the unscaled field
+  // stage-2 epilogue
+  int epilogue;            // 0: weighted intensity reduced into wbuf, 1: complex128 out
+  const double* weights;   // [batch][L] (intensity) -- may be null (weight 1)
+  const double* unit2;     // [L] |alpha_r alpha_c| (or 1)
+  float* wbuf;             // intensity: [batch][M][ldw] FP32 window, zeroed by the caller
+  int ldw;                 // multiple of 4
+  double* out;             // complex: [M][N] double2
+  double complex_scale;    // complex epilogue: extra scale (unitary factor)
+  int* err;                // device error flag
+  cudaEvent_t* events;     // optional [4]: recorded around the stage-1 and stage-2 launches
+};
+int launch_split_mft(const SplitMftProblem& p, cudaStream_t s);
+// scale applied to the stage-1 result before its 16-bit split
+float split_g_scale(int m);
+// out[b][win] += wbuf[b] (FP32 window -> float64 image)
+int launch_window_add(const float* wbuf, int M, int N, int ldw, int batch, double* out, int ld_out,
+                      long long out_bs, int win_r0, int win_c0, cudaStream_t s);
+
+}  // namespace lgb

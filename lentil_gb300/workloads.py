@@ -1,0 +1,86 @@
+"""Seeded synthetic inputs of the benchmark workloads (host-side numpy).
+
+``broadband_segmented`` builds the broadband segmented PSF workload: a
+1024 x 1024 pupil of 18 hexagonal segments (two rings around an empty
+centre, 2 px gaps), per-segment piston/tip/tilt ~ N(0, 50 nm) on each
+segment's own Zernike coordinates, global Noll 2-22 ~ N(0, 15 nm),
+64 wavelengths uniform over 500-900 nm weighted by a 5800 K blackbody
+(photon units, normalised), a 1 m aperture over the pupil grid, f = 10 m,
+5 um detector pixels, 512 x 512 detector at oversample 2.
+
+``monochromatic_circle`` builds the monochromatic 256 x 256 circular
+pupil (diameter 256 px = 1 m, f = 10 m), Noll 2-11 ~ N(0, 20 nm) at
+650 nm onto a 128 x 128 detector of 5 um pixels at oversample 2.
+"""
+import numpy as np
+
+from . import shapes, util
+from .wfe import blackbody_photlam
+from .zernike import zernike as zernike_mode, zernike_coordinates
+
+
+class Workload:
+    """Pupil geometry, OPD basis and spectrum of one benchmark case."""
+
+    def __init__(self, name, amp, mask3d, opd_basis, coeff_sigma, wavelengths, weights,
+                 pixelscale_in, focal_length, det_pixelscale, det_shape, oversample, seed):
+        self.name = name
+        self.amp = amp                  # amplitude, mask applied, power normalised
+        self.mask3d = mask3d            # (S, H, W) segment masks or None
+        self.opd_basis = opd_basis      # (K, H, W) float32 OPD modes
+        self.coeff_sigma = coeff_sigma  # (K,) metres rms per mode
+        self.wavelengths = wavelengths
+        self.weights = weights
+        self.pixelscale_in = pixelscale_in
+        self.focal_length = focal_length
+        self.det_pixelscale = det_pixelscale
+        self.det_shape = det_shape
+        self.oversample = oversample
+        self.seed = seed
+
+    @property
+    def plane_shape(self):
+        return self.amp.shape
+
+    def opds(self, count, seed=None):
+        """``count`` seeded OPD maps (float64, metres)."""
+        rng = np.random.default_rng(self.seed if seed is None else seed)
+        c = rng.normal(0.0, 1.0, (count, len(self.coeff_sigma))) * self.coeff_sigma[None, :]
+        K, H, W = self.opd_basis.shape
+        out = (c.astype(np.float32) @ self.opd_basis.reshape(K, H * W)).reshape(count, H, W)
+        return out.astype(np.float64)
+
+
+def broadband_segmented(npix=1024, n_wavelengths=64, seed=2, seg_radius=None):
+    """The broadband segmented workload (see module docstring)."""
+    if seg_radius is None:
+        seg_radius = 116.8 * npix / 1024
+    segs = shapes.hex_segments(rings=2, seg_radius=seg_radius, seg_gap=2)
+    segs = np.asarray([util.pad(s, (npix, npix)) for s in segs])
+    gmask = segs.sum(axis=0)
+    amp = util.normalize_power(gmask)
+    basis, sigma = [], []
+    for s in segs:
+        rho, theta = zernike_coordinates(s)
+        for j in (1, 2, 3):                       # piston, tip, tilt of this segment
+            basis.append(zernike_mode(s, j, rho=rho, theta=theta).astype(np.float32))
+            sigma.append(50e-9)
+    rho, theta = zernike_coordinates(gmask)
+    for j in range(2, 23):                        # global Noll 2-22
+        basis.append(zernike_mode(gmask, j, rho=rho, theta=theta).astype(np.float32))
+        sigma.append(15e-9)
+    wl_nm = np.linspace(500.0, 900.0, n_wavelengths)
+    w = blackbody_photlam(wl_nm, 5800.0)
+    return Workload('broadband_segmented', amp, segs, np.asarray(basis), np.asarray(sigma),
+                    wl_nm * 1e-9, w / w.sum(), 1.0 / npix, 10.0, 5e-6, npix // 2, 2, seed)
+
+
+def monochromatic_circle(seed=1):
+    """The monochromatic circular-pupil workload (see module docstring)."""
+    npix = 256
+    amp = util.normalize_power(shapes.circle((npix, npix), npix // 2, antialias=False))
+    rho, theta = zernike_coordinates(amp)
+    basis = np.asarray([zernike_mode(amp, j, rho=rho, theta=theta).astype(np.float32)
+                        for j in range(2, 12)])
+    return Workload('monochromatic_circle', amp, None, basis, np.full(10, 20e-9),
+                    np.array([650e-9]), np.array([1.0]), 1.0 / npix, 10.0, 5e-6, 128, 2, seed)

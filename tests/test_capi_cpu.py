@@ -1,0 +1,70 @@
+"""C ABI checks that need no GPU: the library builds, loads and exports every
+symbol include/lentil_gb300.h declares; host-side validation errors map to
+lentil's exception types."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from lentil_gb300 import _build, _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), 'include',
+                      'lentil_gb300.h')
+
+
+def header_functions():
+    text = open(HEADER).read()
+    text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
+    return sorted(set(re.findall(r'\b(lgb_[a-z0-9_]+)\s*\(', text)))
+
+
+@pytest.fixture(scope='module')
+def lib():
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    names = header_functions()
+    assert 'lgb_dft2' in names and 'lgb_psf_execute' in names and 'lgb_phasor' in names
+
+
+def test_library_exports_every_header_symbol(lib):
+    missing = [n for n in header_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_ctypes_signatures_cover_header():
+    assert set(header_functions()) == set(_lib.SIGNATURES)
+
+
+def test_version_and_error_string(lib):
+    assert lib.lgb_version() >> 16 == 1
+    assert isinstance(lib.lgb_last_error(), bytes)
+
+
+def test_invalid_sizes_raise_valueerror(lib):
+    # rejected by host-side validation before any CUDA call
+    st = lib.lgb_dft2(None, 0, 4, None, 4, 4, 0.1, 0.1, 0, 0, 0, 0, 1, 0, None, 0, None)
+    assert st == _lib.EINVAL
+    with pytest.raises(ValueError):
+        _lib.check(st)
+    assert b'positive' in lib.lgb_last_error()
+
+
+def test_unknown_precision_rejected(lib):
+    with pytest.raises(ValueError):
+        _lib.precision_code('fp8')
+    assert lib.lgb_dft2_workspace_size(0, 1, 1, 1, 0) == 0
+
+
+def test_workspace_sizes_are_consistent(lib):
+    a = lib.lgb_dft2_workspace_size(100, 90, 128, 120, _lib.FP64)
+    assert a >= 16 * (128 * 100 + 90 * 120)
+    b = lib.lgb_dft2_workspace_size(100, 90, 128, 120, _lib.SPLIT_BF16)
+    assert b > 0
+    assert lib.lgb_idft2_workspace_size(100, 90, 128, 120, 0) >= a + 16 * 100 * 90
+
+
+def test_build_is_up_to_date():
+    assert _build.up_to_date()

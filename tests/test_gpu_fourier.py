@@ -1,0 +1,125 @@
+"""dft2 / idft2 / DFT matrices on the GPU against lentil's golden vectors and
+the oracle.  Tolerances: complex128 path <= 1e-12 peak-normalised; split
+paths bounded by their 16-bit hi/lo representation (stated per test)."""
+import numpy as np
+import pytest
+import torch
+
+import lentil_gb300 as lg
+from oracle import lentil_oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+SPLIT_TOL = {'split-bf16': 3e-5, 'split-fp16': 2e-6}
+
+
+def _case(g, name):
+    return dict(f=g[f'{name}_f'], alpha=g[f'{name}_alpha'], shape=tuple(g[f'{name}_shape']),
+                shift=g[f'{name}_shift'], offset=g[f'{name}_offset'],
+                unitary=bool(g[f'{name}_unitary']))
+
+
+def test_dft2_fp64_golden(golden, cuda_device):
+    g = golden('dft2')
+    for name in g['names']:
+        c = _case(g, name)
+        F = lg.fourier.dft2(c['f'], c['alpha'], shape=c['shape'], shift=c['shift'],
+                            offset=c['offset'], unitary=c['unitary'])
+        assert isinstance(F, np.ndarray) and F.dtype == np.complex128
+        assert lo.peak_normalised_error(F, g[f'{name}_F']) < FP64_TOL, name
+
+
+@pytest.mark.parametrize('precision', ['split-bf16', 'split-fp16'])
+def test_dft2_split_golden(golden, cuda_device, precision):
+    g = golden('dft2')
+    for name in g['names']:
+        c = _case(g, name)
+        F = lg.fourier.dft2(c['f'], c['alpha'], shape=c['shape'], shift=c['shift'],
+                            offset=c['offset'], unitary=c['unitary'], precision=precision)
+        e = lo.peak_normalised_error(F, g[f'{name}_F'])
+        assert e < SPLIT_TOL[precision], (name, e)
+
+
+def test_dft2_shift_centroid_and_offset(golden, cuda_device):
+    g = golden('dft2')
+    n = 100
+    F = lg.fourier.dft2(np.ones((n, n)), 1 / n, shift=g['shift100_shift'])
+    assert lo.peak_normalised_error(F, g['shift100_F']) < FP64_TOL
+    c = np.asarray(lo.centroid(np.abs(F) ** 2)) - n // 2
+    assert np.allclose(c, g['shift100_shift'], atol=1e-9)
+    f = g['offset_f']
+    r0, r1, c0, c1 = g['offset_slice']
+    FF = lg.fourier.dft2(f[r0:r1, c0:c1], alpha=1 / 3, shape=10, offset=g['offset_offset'])
+    assert lo.peak_normalised_error(FF, g['offset_F']) < FP64_TOL
+
+
+def test_idft2_golden(golden, cuda_device):
+    g = golden('dft2')
+    for name, n in (('ieven', 10), ('iodd', 11)):
+        f = lg.fourier.idft2(g[f'{name}_F'], 1 / n, unitary=False)
+        assert lo.peak_normalised_error(f, g[f'{name}_f']) < FP64_TOL
+
+
+def test_dft2_matches_fft(cuda_device):
+    # lentil's own known-answer test (tests/test_fourier.py:7-44): alpha=1/n
+    # equals the shifted FFT, even and odd sizes, rectangular
+    rng = np.random.default_rng(3)
+    for m, n in ((10, 10), (11, 11), (10, 11), (64, 48)):
+        f = rng.random((m, n)) + 1j * rng.random((m, n))
+        F = lg.fourier.dft2(f, [1 / m, 1 / n], unitary=False)
+        Ff = np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(f)))
+        assert np.allclose(F, Ff, rtol=1e-11, atol=1e-11)
+        fi = lg.fourier.idft2(f, [1 / m, 1 / n], unitary=False)
+        fif = np.fft.fftshift(np.fft.ifft2(np.fft.ifftshift(f)))
+        assert np.allclose(fi, fif, rtol=1e-11, atol=1e-13)
+
+
+def test_dft2_unitary_parseval_and_inverse(cuda_device):
+    rng = np.random.default_rng(4)
+    f = rng.random((10, 10)) + 1j * rng.random((10, 10))
+    F = lg.fourier.dft2(f, 1 / 10, unitary=True)
+    assert np.isclose(np.sum(np.abs(f) ** 2), np.sum(np.abs(F) ** 2), rtol=1e-13)
+    F = lg.fourier.dft2(f, 1 / 10, unitary=False)
+    assert np.allclose(lg.fourier.idft2(F, 1 / 10, unitary=False), f, rtol=1e-12, atol=1e-13)
+
+
+def test_dft2_out_and_npix(cuda_device):
+    rng = np.random.default_rng(5)
+    f = rng.normal(size=(10, 10)).astype(complex)
+    F = lg.fourier.dft2(f, 1 / 10, out=f)
+    assert F is f
+    g = rng.normal(size=(12, 9)) + 0j
+    a = lg.fourier.dft2(g, 0.05, npix=(14, 15))
+    b = lg.fourier.dft2(g, 0.05, shape=(14, 15))
+    assert np.array_equal(a, b) and a.shape == (14, 15)
+    with pytest.raises(TypeError):
+        lg.fourier.dft2(g, 0.05, out=np.zeros((12, 9), dtype=float))
+    t = torch.as_tensor(g, device='cuda')
+    T = lg.fourier.dft2(t, 0.05, npix=(14, 15))
+    assert isinstance(T, torch.Tensor) and T.is_cuda
+    assert np.array_equal(T.cpu().numpy(), a)
+
+
+def test_dft2_matrices_match_oracle(cuda_device):
+    E1, E2 = lg.fourier.dft2_matrices(37, 29, 41, 33, (0.0123, -0.0071), shift=(3.25, -7.5),
+                                      offset=(-4.5, 2.0))
+    O1, O2 = lo.dft2_matrices(37, 29, 41, 33, 0.0123, -0.0071, 3.25, -7.5, -4.5, 2.0)
+    assert np.max(np.abs(E1.cpu().numpy() - O1)) < 1e-12
+    assert np.max(np.abs(E2.cpu().numpy() - O2)) < 1e-12
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split-bf16', 'split-fp16'])
+def test_dft2_config_sizes(cuda_device, precision):
+    # 1024-pupil-sized transforms (the broadband workload's per-wavelength MFT)
+    rng = np.random.default_rng(6)
+    m = n = 300
+    amp = lo.normalize_power(lg.circle((m, n), 140))
+    f = amp * np.exp(2j * np.pi * rng.normal(0, 0.05, (m, n)))
+    alpha = (1 / 300) * 5e-6 / (600e-9 * 10 * 2)
+    F = lg.fourier.dft2(f, alpha, shape=(256, 320), shift=(0.3, -0.6), offset=(2, -3),
+                        precision=precision)
+    Fo = lo.dft2(f, alpha, shape=(256, 320), shift=(0.3, -0.6), offset=(2, -3))
+    e = lo.peak_normalised_error(np.abs(F) ** 2, np.abs(Fo) ** 2)
+    tol = {'fp64': 1e-12, 'split-bf16': 1e-6, 'split-fp16': 1e-6}[precision]
+    assert e < tol, e

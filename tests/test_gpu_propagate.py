@@ -1,0 +1,193 @@
+"""propagate_dft, Plane phasors, field algebra and the fused broadband plan on
+the GPU against lentil's golden vectors and the oracle."""
+import numpy as np
+import pytest
+import torch
+
+import lentil_gb300 as lg
+from oracle import lentil_oracle as lo
+from tests.golden_cases import PROPAGATE_CASES, build_pupil, propagate_kwargs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize('name', PROPAGATE_CASES)
+def test_propagate_fp64_golden(golden, cuda_device, name):
+    g = golden('propagate')
+    pl = build_pupil(lg, g, name)
+    w = lg.propagate_dft(lg.Wavefront(float(g[f'{name}_wavelength'])) * pl,
+                         **propagate_kwargs(g, name))
+    assert len(w.data) == int(g[f'{name}_nfields'])
+    I = w.intensity
+    ref = g[f'{name}_intensity']
+    assert isinstance(I, np.ndarray) and I.shape == ref.shape
+    if np.max(ref) == 0:
+        assert np.all(I == 0)
+    else:
+        assert lo.peak_normalised_error(I, ref) < 1e-12
+
+
+# split tolerances: two 16-bit planes give 16 (bf16) or 22 (fp16) significant
+# bits per operand, and the FP32 tensor-core accumulation is folded into
+# round-to-nearest registers every two MMA k-steps
+SPLIT_TOL = {'split-bf16': 3e-5, 'split-fp16': 2e-6}
+
+
+@pytest.mark.parametrize('precision', ['split-bf16', 'split-fp16'])
+@pytest.mark.parametrize('name', ['config1', 'tilt_fit1', 'oddrect', 'seg_fit0', 'seg_fit1'])
+def test_propagate_split_golden(golden, cuda_device, name, precision):
+    g = golden('propagate')
+    pl = build_pupil(lg, g, name)
+    w = lg.propagate_dft(lg.Wavefront(float(g[f'{name}_wavelength'])) * pl,
+                         precision=precision, **propagate_kwargs(g, name))
+    e = lo.peak_normalised_error(w.intensity, g[f'{name}_intensity'])
+    assert e < SPLIT_TOL[precision], e
+
+
+def test_plane_phasor_matches_oracle(cuda_device):
+    rng = np.random.default_rng(1)
+    amp = rng.uniform(size=(10, 10))
+    opd = rng.uniform(size=(10, 10))
+    p = lg.Plane(pixelscale=1, amplitude=amp, opd=opd)
+    w = lg.Wavefront(650e-9) * p
+    slc = lo.boundary_slice(amp.astype(bool))
+    ref = amp[slc] * np.exp(2 * np.pi * 1j * opd[slc] / 650e-9)
+    d = w.data[0].data.cpu().numpy()
+    # lentil's own test uses OPDs of up to 1 m: the phase argument reaches
+    # 1e7 rad, so both evaluations carry ~1e-16 * 1e7 absolute phase error
+    phase_max = 2 * np.pi * np.max(opd) / 650e-9
+    assert np.max(np.abs(d - ref)) < 4e-16 * phase_max * np.max(np.abs(ref))
+
+
+def test_overlapping_segment_slices(cuda_device):
+    # lentil tests/test_plane.py:117-131
+    seg = lg.hexagon((64, 64), 32, antialias=False)[5:60, :]
+    segmask = np.zeros((2, 128, 128))
+    segmask[0, 0:55, 2:66] = seg
+    segmask[1, 29:84, 55:119] = seg
+    mask = np.sum(segmask, axis=0)
+    pupil = lg.Pupil(amplitude=mask, mask=segmask, pixelscale=1 / 256, focal_length=10)
+    w = lg.Wavefront(500e-9)
+    w *= pupil
+    assert np.allclose(mask, w.intensity, rtol=0, atol=1e-12)
+
+
+def test_field_algebra_golden(golden, cuda_device):
+    g = golden('field')
+    a = lg.Field(np.ones((5, 4)), pixelscale=1, offset=[-2, -2])
+    b = lg.Field(np.ones((3, 3)), pixelscale=1, offset=[0, -1])
+    c = lg.field.merge(a, b)
+    assert np.array_equal(c.data.cpu().numpy(), g['merge_data'])
+    assert np.array_equal(c.offset, g['merge_offset'])
+    fs = [lg.Field(g[f'reduce_in{k}_data'], pixelscale=1, offset=list(g[f'reduce_in{k}_offset']))
+          for k in range(4)]
+    red = lg.field.reduce(fs)
+    assert len(red) == int(g['reduce_n'])
+    for k, f in enumerate(red):
+        assert np.allclose(f.data.cpu().numpy(), g[f'reduce_out{k}_data'], rtol=0, atol=1e-15)
+        assert np.array_equal(f.offset, g[f'reduce_out{k}_offset'])
+    out = np.zeros((9, 8))
+    for f in fs:
+        out = lg.field.insert(f, out, intensity=True, weight=0.7)
+    assert np.allclose(out, g['insert_intensity'], rtol=1e-14, atol=0)
+    out = np.zeros((9, 8), dtype=complex)
+    for f in fs:
+        out = lg.field.insert(f, out)
+    assert np.allclose(out, g['insert_complex'], rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize('case', [
+    (1, [0, 0], 1, [0, 0], 1 + 0j, [0, 0]),
+    (1, [0, 0], 1, [1, 0], [], [0, 0]),
+    (np.ones((2, 2)), [0, 0], np.ones((2, 2)), [0, 0], np.ones((2, 2)), [0, 0]),
+    (np.ones((2, 2)), [0, 0], np.ones((2, 2)), [4, 4], [], [0, 0]),
+    (1, [0, 0], np.ones((3, 3)), [-5, -5], np.ones((3, 3)), [-5, -5]),
+    (np.ones((5, 4)), [-2, -2], np.ones((3, 3)), [0, -1], np.ones((2, 2)), [0, -1]),
+])
+def test_field_multiply(cuda_device, case):
+    # lentil tests/test_field.py:7-24
+    a_data, a_off, b_data, b_off, data, off = case
+    c = lg.Field(a_data, pixelscale=1, offset=a_off) * lg.Field(b_data, pixelscale=1, offset=b_off)
+    assert np.array_equal(c.data.cpu().numpy(), np.asarray(data, dtype=complex))
+    if c.size:
+        assert np.array_equal(c.offset, off)
+
+
+def test_default_wavefront(cuda_device):
+    w = lg.Wavefront(wavelength=500e-9)
+    assert np.array_equal(w.field, 1 + 0j)
+    assert np.array_equal(w.intensity, 1)
+    with pytest.raises(TypeError):
+        lg.propagate_dft(w, shape=(64, 64), pixelscale=5e-6)
+
+
+def _bb_pupil(golden):
+    g = golden('propagate')
+    return g, dict(amplitude=g['bb_amp'], opd=g['bb_opd'], pixelscale=g['bb_pixelscale_in'].tolist(),
+                   focal_length=10)
+
+
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-12), ('split-bf16', 2e-6),
+                                           ('split-fp16', 5e-7)])
+def test_broadband_plan_golden(golden, cuda_device, precision, tol):
+    g, kw = _bb_pupil(golden)
+    img = lg.broadband_psf(lg.Pupil(**kw), g['bb_wl'], g['bb_wt'], 6e-6, shape=24, oversample=2,
+                           precision=precision)
+    e = lo.peak_normalised_error(img, g['bb_img'])
+    assert e < tol, e
+
+
+def test_broadband_loop_equals_plan(golden, cuda_device):
+    # the user loop through propagate_dft + Wavefront.insert and the fused plan
+    g, kw = _bb_pupil(golden)
+    pl = lg.Pupil(**kw)
+    img = np.zeros((48, 48))
+    for lam, w in zip(g['bb_wl'], g['bb_wt']):
+        img = lg.propagate_dft(lg.Wavefront(lam) * pl, 6e-6, shape=24, oversample=2).insert(img, w)
+    assert lo.peak_normalised_error(img, g['bb_img']) < 1e-12
+    fused = lg.broadband_psf(pl, g['bb_wl'], g['bb_wt'], 6e-6, shape=24, oversample=2,
+                             precision='fp64')
+    assert lo.peak_normalised_error(fused, img) < 1e-12
+
+
+@pytest.mark.parametrize('fit', [False, True])
+def test_broadband_segmented(golden, cuda_device, fit):
+    # 3-D segment mask: merged dense field (no tilts) or per-segment fields
+    g = golden('propagate')
+    name = f'seg_fit{int(fit)}'
+    wl = np.array([500e-9, 550e-9, 640e-9])
+    wt = np.array([0.3, 0.3, 0.4])
+    pl = build_pupil(lg, g, name)
+    po = build_pupil(lo, g, name)
+    kw = propagate_kwargs(g, name)
+    ref = lo.broadband_psf(po, wl, wt, **kw)
+    for prec, tol in (('fp64', 1e-12), ('split-bf16', 2e-5)):
+        img = lg.broadband_psf(pl, wl, wt, precision=prec, **kw)
+        assert lo.peak_normalised_error(img, ref) < tol, prec
+
+
+def test_plan_batch_matches_single(cuda_device):
+    # PSFs of a batch equal the same PSFs computed alone
+    rng = np.random.default_rng(9)
+    H = 96
+    amp = lo.normalize_power(lg.circle((H, H), 44))
+    wl = np.linspace(500e-9, 800e-9, 5)
+    alphas = [((1 / 88) * 5e-6 / (l * 10 * 2),) * 2 for l in wl]
+    shifts = [(0.0, 0.0)] * len(wl)
+    B = 3
+    opd = np.stack([lg.zernike_compose(amp, np.r_[0, rng.normal(0, 30e-9, 10)]) for _ in range(B)])
+    wts = rng.uniform(0.5, 1.5, (B, len(wl)))
+    A = torch.as_tensor(np.broadcast_to(amp, (B, H, H)).copy(), device='cuda')
+    O = torch.as_tensor(opd, device='cuda')
+    for prec in ('fp64', 'split-bf16'):
+        plan = lg.PSFPlan((H, H), (0, 0, H, H), (0, 0), wl, alphas, shifts, (80, 72), (80, 72),
+                          (0, 0), batch=B, precision=prec)
+        outb = plan.execute(A, O, wts).cpu().numpy()
+        one = lg.PSFPlan((H, H), (0, 0, H, H), (0, 0), wl, alphas, shifts, (80, 72), (80, 72),
+                         (0, 0), batch=1, precision=prec)
+        for b in range(B):
+            o1 = one.execute(A[b:b + 1].contiguous(), O[b:b + 1].contiguous(), wts[b:b + 1]).cpu().numpy()
+            # the split path reduces wavelengths into FP32 with atomic adds,
+            # whose order is not fixed: equal to FP32 rounding, not bitwise
+            tol = 1e-12 if prec == 'fp64' else 1e-6
+            assert lo.peak_normalised_error(outb[b], o1[0]) < tol
