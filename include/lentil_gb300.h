@@ -74,6 +74,24 @@ int lgb_dft2(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int N,
 int lgb_dft2_status(void* workspace, lgb_stream stream);
 
 /* ------------------------------------------------------------------------
+ * Allocation-free complex128 dft2 (no counterpart in lentil: an addition of
+ * this library for callers that may not allocate device memory at call time,
+ * e.g. a control loop with a fixed memory budget or work issued into a
+ * stream under graph capture).  Same arguments and result as lgb_dft2 with
+ * precision LGB_FP64, but the scratch comes from a fixed array inside the
+ * library (LGB_NOALLOC_SCRATCH_BYTES, held by every GPU that loads it) and
+ * the caller passes only f and F.  Transforms needing more scratch than that
+ * (lgb_dft2_workspace_size(m, n, M, N, LGB_FP64) bytes) are rejected with
+ * LGB_EINVAL.  The first call on a device looks the array's address up with
+ * cudaGetSymbolAddress; make it outside any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race.
+ * ---------------------------------------------------------------------- */
+#define LGB_NOALLOC_SCRATCH_BYTES (16u << 20)
+int lgb_dft2_noalloc(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int N,
+                     double alpha_r, double alpha_c, double shift_r, double shift_c,
+                     double offset_r, double offset_c, int unitary, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
  * Inverse MFT.  Replaces lentil/fourier.py:124-198 (idft2):
  *   f = conj(dft2(conj(F), alpha, shape, shift, unitary)) / F.size
  * F is m x n, f is M x N.  Workspace: lgb_idft2_workspace_size bytes.
