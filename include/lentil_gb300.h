@@ -139,6 +139,27 @@ int lgb_field_multiply(const lgb_c128* a, int lda, int ar0, int ac0,
                        lgb_c128* out, int om, int on, lgb_stream stream);
 
 /* ------------------------------------------------------------------------
+ * Detector pixel MTF.  Replaces lentil/detector.py:167-222 (pixel):
+ *   out = |ifft2(fft2(img) * outer(s, s))|,  s = sinc(fftfreq(N) * os),
+ * evaluated as |C . img . C^T| with C the real circulant of ifft(s) (FP64).
+ * img and out are N x N float64 (lentil defines it for square images only;
+ * rows != cols -> LGB_EINVAL).  Workspace: lgb_pixel_workspace_size bytes.
+ * ---------------------------------------------------------------------- */
+size_t lgb_pixel_workspace_size(int N, int oversample);
+int lgb_pixel(const double* img, int rows, int cols, int oversample, double* out,
+              void* workspace, size_t workspace_bytes, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Pixelation.  Replaces lentil/detector.py:225-251 (pixelate = pixel, then
+ * lentil/util.py:261-349 rescale(1/os, order=3, mode='nearest',
+ * unitary=True)).  For N a multiple of os every resample point is a grid
+ * point, so out (N/os x N/os) = p[::os, ::os] * sum(p)/sum(p[::os, ::os]),
+ * zero where the sample is zero.  N % os != 0 -> LGB_EUNSUPPORTED.
+ * ---------------------------------------------------------------------- */
+int lgb_pixelate(const double* img, int rows, int cols, int oversample, double* out,
+                 void* workspace, size_t workspace_bytes, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
  * Broadband PSF plan: the documented user loop
  *   for lam, w: img = propagate_dft(Wavefront(lam) * pupil, ...).insert(img, w)
  * (docs/user/performance.rst:44-49) fused for a batch of PSFs that share the

@@ -13,6 +13,7 @@ __version__ = '0.1.0'
 
 from .ptype import ptype, none, pupil, image, tilt, transform
 from . import fourier
+from . import detector
 from . import field
 from .field import Field
 from .plane import Plane, Pupil, Image, Tilt

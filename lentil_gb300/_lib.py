@@ -53,6 +53,10 @@ SIGNATURES = {
                                  c_double, c_int, c_void_p]),
     'lgb_field_multiply': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int, c_int,
                                    c_void_p, c_int, c_int, c_void_p]),
+    'lgb_pixel_workspace_size': (c_size_t, [c_int, c_int]),
+    'lgb_pixel': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
+    'lgb_pixelate': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t,
+                             c_void_p]),
     'lgb_psf_plan_create': (c_int, [ctypes.POINTER(PsfDesc), ctypes.POINTER(c_void_p), c_void_p]),
     'lgb_psf_plan_bytes': (c_size_t, [c_void_p]),
     'lgb_psf_execute': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),

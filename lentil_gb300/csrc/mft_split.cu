@@ -45,7 +45,10 @@ namespace tc {
 
 constexpr int BM = 128, BN = 256, BK = 64, STAGES = 2;
 constexpr int KSTEPS = BK / 16;                            // MMA k-steps per K block
-constexpr int KSUB = 2;                                    // k-steps per hi.hi chain
+#ifndef LGB_KSUB
+#define LGB_KSUB 2
+#endif
+constexpr int KSUB = LGB_KSUB;                             // k-steps per hi.hi chain
 constexpr int CHUNKS = KSTEPS / KSUB;                      // X chunks per K block
 constexpr uint32_t A_BYTES = BM * BK * 2;                  // 16 KB per plane
 constexpr uint32_t B_BYTES = BN * BK * 2;                  // 32 KB per plane

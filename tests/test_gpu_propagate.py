@@ -191,3 +191,23 @@ def test_plan_batch_matches_single(cuda_device):
             # whose order is not fixed: equal to FP32 rounding, not bitwise
             tol = 1e-12 if prec == 'fp64' else 1e-6
             assert lo.peak_normalised_error(outb[b], o1[0]) < tol
+
+
+@pytest.mark.parametrize('name', ['px64os2', 'px90os3', 'px128os4'])
+def test_pixel_pixelate_golden(golden, cuda_device, name):
+    # lentil/detector.py:167-251 against lentil's own outputs
+    g = golden('detector')
+    img, os_ = g[f'{name}_img'], int(g[f'{name}_os'])
+    assert lo.peak_normalised_error(lg.detector.pixel(img, os_), g[f'{name}_pixel']) < 1e-12
+    assert lo.peak_normalised_error(lg.detector.pixelate(img, os_), g[f'{name}_pixelate']) < 1e-12
+
+
+def test_pixel_unitary_and_errors(cuda_device):
+    # lentil tests/test_detector.py:86-97
+    a = np.random.default_rng(2).uniform(0, 1, (100, 100))
+    assert np.isclose(np.sum(a), np.sum(lg.detector.pixel(a, oversample=1)), rtol=1e-12)
+    assert lg.detector.pixelate(np.ones((10, 10)), 2).shape == (5, 5)
+    with pytest.raises(ValueError):
+        lg.detector.pixel(np.ones((10, 12)), 2)
+    with pytest.raises(NotImplementedError):
+        lg.detector.pixelate(np.ones((10, 10)), 3)
