@@ -50,6 +50,10 @@ def parse():
                     help='wavelengths in the bounded CPU-baseline sample')
     ap.add_argument('--npix', type=int, default=1024)
     ap.add_argument('--wavelengths', type=int, default=64)
+    ap.add_argument('--workload', default='broadband',
+                    choices=['broadband', 'monochromatic', 'phase_retrieval'],
+                    help='broadband: the headline workload; the others measure the '
+                         'monochromatic 256^2 PSF and the focus-diverse gradient')
     return ap.parse_args()
 
 
@@ -379,10 +383,133 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def _timed(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    s = torch.cuda.current_stream()
+    for a, b in ev:
+        a.record(s)
+        fn()
+        b.record(s)
+    torch.cuda.synchronize()
+    ms = sorted(a.elapsed_time(b) for a, b in ev)
+    return statistics.mean(ms), statistics.median(ms), float(np.percentile(ms, 99))
+
+
+def run_monochromatic(args):
+    """256^2 circular pupil, Noll 2-11, 650 nm, 128^2 detector x2: lentil's
+    propagate_dft + intensity through the drop-in API (complex128) and the
+    fused plan (split), against the oracle."""
+    import torch
+    import lentil_gb300 as lg
+    from lentil_gb300 import broadband, workloads
+    from oracle import lentil_oracle as lo
+    wl = workloads.monochromatic_circle()
+    opd = wl.opds(1)[0]
+    pl = lg.Pupil(amplitude=wl.amp, opd=opd, pixelscale=wl.pixelscale_in, focal_length=wl.focal_length)
+    api = lambda: lg.propagate_dft(lg.Wavefront(650e-9) * pl, wl.det_pixelscale, shape=wl.det_shape,
+                                   oversample=wl.oversample).intensity_tensor()
+    api_mean, api_p50, api_p99 = _timed(api, args.steps, args.warmup)
+    s = lg.util.boundary_slice(wl.amp)
+    geo = broadband.plan_geometry(wl.plane_shape, s, [], np.broadcast_to(wl.pixelscale_in, (2,)),
+                                  wl.focal_length, lg.pupil, wl.wavelengths, wl.det_pixelscale,
+                                  shape=wl.det_shape, oversample=wl.oversample)
+    plan = broadband.make_plan(geo, batch=1, precision=args.precision)
+    A = torch.as_tensor(wl.amp[None], device='cuda')
+    O = torch.as_tensor(opd[None], device='cuda')
+    W = torch.ones((1, 1), dtype=torch.float64, device='cuda')
+    out = torch.empty((1,) + geo.shape_out, dtype=torch.float64, device='cuda')
+    fused = lambda: plan.execute(A, O, W, out=out, check=False)
+    f_mean, f_p50, f_p99 = _timed(fused, args.steps, args.warmup)
+    ref_pl = lo.Pupil(amplitude=wl.amp, opd=opd, pixelscale=wl.pixelscale_in, focal_length=wl.focal_length)
+    t0 = time.perf_counter()
+    ref = lo.propagate_dft(lo.Wavefront(650e-9) * ref_pl, wl.det_pixelscale, shape=wl.det_shape,
+                           oversample=wl.oversample).intensity
+    cpu_s = time.perf_counter() - t0
+    e_api = lo.peak_normalised_error(api().cpu().numpy(), ref)
+    e_fused = lo.peak_normalised_error(plan.execute(A, O, W).cpu().numpy()[0], ref)
+    line = {'metric': 'monochromatic 256^2 PSFs/s', 'value': 1e3 / f_mean, 'unit': 'PSFs/s',
+            'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': f_mean,
+            'p50_ms': f_p50, 'p99_ms': f_p99, 'higher_is_better': True,
+            'dtype': args.precision, 'data': 'synthetic (seeded)',
+            'config': {'workload': 'monochromatic 256^2 circular pupil, Noll 2-11 N(0,20nm), '
+                                   '650 nm, 128^2 detector x oversample 2'},
+            'api_fp64': {'value': 1e3 / api_mean, 'p50_ms': api_p50, 'p99_ms': api_p99,
+                         'err_vs_oracle': e_api},
+            'err_vs_oracle': e_fused,
+            'cpu_baseline': {'value': 1.0 / cpu_s, 'unit': 'PSFs/s', 'cores': os.cpu_count(),
+                             'kind': 'port', 'sample': 'one PSF through the oracle'}}
+    print(json.dumps(line), flush=True)
+
+
+def run_phase_retrieval(args):
+    """512^2 circular pupil, OPD = Noll 2-37 N(0,30nm) + 18-segment PTT
+    N(0,40nm), three images at defocus -1/0/+1 wave P-V (633 nm), 256^2
+    detector x2: one loss + gradient evaluation per step."""
+    import torch
+    import lentil_gb300 as lg
+    from lentil_gb300 import autodiff
+    npix = 512
+    amp = lg.normalize_power(lg.circle((npix, npix), npix // 2))
+    support = amp > 0
+    segs = lg.hex_segments(rings=2, seg_radius=116.8 * npix / 1024 * 1.0, seg_gap=2)
+    segs = np.asarray([lg.pad(x, (npix, npix)) for x in segs]) * support
+    basis, sigma = [], []
+    rho, th = lg.zernike_coordinates(support)
+    for j in range(2, 38):
+        basis.append(lg.zernike(support, j, rho=rho, theta=th)); sigma.append(30e-9)
+    for sg in segs:
+        if sg.sum() == 0:
+            continue
+        r2, t2 = lg.zernike_coordinates(sg)
+        for j in (1, 2, 3):
+            basis.append(lg.zernike(sg, j, rho=r2, theta=t2)); sigma.append(40e-9)
+    basis, sigma = np.asarray(basis), np.asarray(sigma)
+    g = autodiff.geometry(amp, 633e-9, 1.0 / npix, 10.0, 5e-6, shape=256, oversample=2,
+                          precision=args.precision)
+    z4 = lg.zernike(support, 4)
+    div = [k * 633e-9 / (z4.max() - z4.min()) * z4 for k in (-1, 0, 1)]
+    rng = np.random.default_rng(4)
+    true_c = rng.normal(0, 1, len(sigma)) * sigma
+    pr = autodiff.PhaseRetrieval(amp, basis, div, [np.zeros(g.shape)] * 3, g)
+    with torch.no_grad():
+        t = [autodiff.mft_intensity(pr.opd(torch.as_tensor(true_c, device='cuda')) + d, pr.amp, g)
+             for d in pr.diversity]
+    pr.targets = [x + 1e-4 * x.max() * torch.as_tensor(rng.normal(size=g.shape), device='cuda')
+                  for x in t]
+    c = torch.zeros(len(sigma), dtype=torch.float64, device='cuda', requires_grad=True)
+
+    def step():
+        c.grad = None
+        pr.loss(c).backward()
+
+    mean, p50, p99 = _timed(step, args.steps, args.warmup)
+    m, n = g.slc[2], g.slc[3]
+    M, N = g.shape
+    flops = 3 * 8.0 * (M * m * n + M * n * N) * 3      # forward + recompute + adjoint, 3 images
+    line = {'metric': 'focus-diverse phase-retrieval loss+gradient evaluations/s',
+            'value': 1e3 / mean, 'unit': 'evals/s', 'n_gpus': 1, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': mean, 'p50_ms': p50, 'p99_ms': p99,
+            'higher_is_better': True, 'dtype': args.precision, 'data': 'synthetic (seeded)',
+            'config': {'workload': '512^2 circular pupil, Noll 2-37 + 18-segment PTT, 3 diversity '
+                                   'images at -1/0/+1 wave defocus, 633 nm, 256^2 detector x2',
+                       'parameters': int(len(sigma))},
+            'mft_tflops_algorithmic': flops / (mean / 1e3) / 1e12}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         run_reference(args)
+    elif args.workload == 'monochromatic':
+        run_monochromatic(args)
+    elif args.workload == 'phase_retrieval':
+        run_phase_retrieval(args)
     else:
         run_gpu(args)
 

@@ -160,6 +160,22 @@ int lgb_pixelate(const double* img, int rows, int cols, int oversample, double* 
                  void* workspace, size_t workspace_bytes, lgb_stream stream);
 
 /* ------------------------------------------------------------------------
+ * Gradient building blocks (no counterpart in lentil, which has no
+ * gradients; they make the MFT path differentiable for phase retrieval).
+ * For I = |F|^2 with F = dft2(f), f = amp exp(2 pi i opd / lambda):
+ *   lgb_abs2:              I = |F|^2                               (count)
+ *   lgb_intensity_adjoint: Hc = dL/dI * conj(F)  (conjugate of dL/dF*)
+ *   then q = dft2(Hc, alpha, shape=(m, n), shift=-offset, offset=-shift)
+ *   (the adjoint MFT: E1^T conj(H) E2^T), and
+ *   lgb_phasor_adjoint:    grad_opd[r0+i, c0+j] += -(4 pi / lambda) Im(q f)
+ * ---------------------------------------------------------------------- */
+int lgb_abs2(const lgb_c128* F, double* I, size_t count, lgb_stream stream);
+int lgb_intensity_adjoint(const lgb_c128* F, const double* grad_I, lgb_c128* Hc, size_t count,
+                          lgb_stream stream);
+int lgb_phasor_adjoint(const lgb_c128* q, const lgb_c128* f, int m, int n, double wavelength,
+                       double* grad_opd, int ld, int r0, int c0, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
  * Broadband PSF plan: the documented user loop
  *   for lam, w: img = propagate_dft(Wavefront(lam) * pupil, ...).insert(img, w)
  * (docs/user/performance.rst:44-49) fused for a batch of PSFs that share the

@@ -57,6 +57,10 @@ SIGNATURES = {
     'lgb_pixel': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
     'lgb_pixelate': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t,
                              c_void_p]),
+    'lgb_abs2': (c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
+    'lgb_intensity_adjoint': (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    'lgb_phasor_adjoint': (c_int, [c_void_p, c_void_p, c_int, c_int, c_double, c_void_p, c_int,
+                                   c_int, c_int, c_void_p]),
     'lgb_psf_plan_create': (c_int, [ctypes.POINTER(PsfDesc), ctypes.POINTER(c_void_p), c_void_p]),
     'lgb_psf_plan_bytes': (c_size_t, [c_void_p]),
     'lgb_psf_execute': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),

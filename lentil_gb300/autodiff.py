@@ -1,0 +1,121 @@
+"""Differentiable MFT intensity for phase retrieval (no counterpart in
+lentil, which has no gradients).
+
+``mft_intensity(opd, amp, ...)`` is lentil's monochromatic PSF
+(``propagate_dft(Wavefront(lam) * Pupil(amp, opd)).intensity``, one field,
+no tilt) as a ``torch.autograd.Function`` of the OPD map.  Forward: phasor
+kernel, MFT (complex128 or split tensor-core), |F|^2.  Backward, with the
+field recomputed instead of stored: dL/dF* = dL/dI * F, the adjoint MFT
+(a dft2 of its conjugate with offset and shift swapped and negated), and
+dL/dopd = (2 pi / lambda) 2 Im(g conj(f)) from the phasor-adjoint kernel.
+"""
+from collections import namedtuple
+
+import numpy as np
+import torch
+
+from . import _device as dv
+from . import _lib
+from . import fourier
+from . import util
+from .propagate import _dft_alpha
+
+Geometry = namedtuple('Geometry', 'wavelength alpha shape shift offset slc plane precision')
+
+
+def geometry(amp, wavelength, pixelscale_in, focal_length, pixelscale_out, shape,
+             oversample=2, precision='fp64'):
+    """MFT geometry of ``propagate_dft`` for an untilted single-field pupil
+    whose support is ``amp != 0`` (lentil/propagate.py:373-438,
+    lentil/plane.py:494-510): full output window, zero shift, slice offset."""
+    a = dv.to_host(amp) if dv.is_tensor(amp) else np.asarray(amp)
+    slc = util.boundary_slice(a != 0)
+    off = util.slice_offset(slc, a.shape)
+    dx = np.broadcast_to(pixelscale_in, (2,))
+    du = np.broadcast_to(pixelscale_out, (2,))
+    shp = np.broadcast_to(shape, (2,)) * oversample
+    alpha = _dft_alpha(dx, du, wavelength, focal_length, oversample)
+    r0, c0 = int(slc[0].start), int(slc[1].start)
+    m, n = int(slc[0].stop) - r0, int(slc[1].stop) - c0
+    return Geometry(float(wavelength), tuple(float(x) for x in alpha),
+                    (int(shp[0]), int(shp[1])), (0.0, 0.0), tuple(int(x) for x in off),
+                    (r0, c0, m, n), tuple(a.shape), precision)
+
+
+def _phasor(amp, opd, g):
+    r0, c0, m, n = g.slc
+    H, W = g.plane
+    f = torch.empty((m, n), dtype=torch.complex128, device=amp.device)
+    _lib.call('lgb_phasor', amp.data_ptr(), 0.0, None, opd.data_ptr(), 0.0, H, W, r0, c0, m, n,
+              g.wavelength, f.data_ptr(), dv.stream_ptr())
+    return f
+
+
+def _forward_field(amp, opd, g):
+    f = _phasor(amp, opd, g)
+    F = fourier.dft2(f, g.alpha, shape=g.shape, shift=g.shift, offset=g.offset, unitary=True,
+                     precision=g.precision)
+    return f, F
+
+
+class MFTIntensity(torch.autograd.Function):
+    """I = |dft2(amp exp(2 pi i opd / lambda))|^2, differentiable in opd."""
+
+    @staticmethod
+    def forward(ctx, opd, amp, g):
+        opd = opd.detach().to(torch.float64).contiguous()
+        amp = amp.detach().to(torch.float64).contiguous()
+        _, F = _forward_field(amp, opd, g)
+        I = torch.empty(F.shape, dtype=torch.float64, device=F.device)
+        _lib.call('lgb_abs2', F.data_ptr(), I.data_ptr(), F.numel(), dv.stream_ptr())
+        ctx.save_for_backward(opd, amp)
+        ctx.g = g
+        return I
+
+    @staticmethod
+    def backward(ctx, grad_I):
+        opd, amp = ctx.saved_tensors
+        g = ctx.g
+        f, F = _forward_field(amp, opd, g)                 # recomputed, not stored
+        gI = grad_I.detach().to(torch.float64).contiguous()
+        Hc = torch.empty_like(F)
+        _lib.call('lgb_intensity_adjoint', F.data_ptr(), gI.data_ptr(), Hc.data_ptr(), F.numel(),
+                  dv.stream_ptr())
+        r0, c0, m, n = g.slc
+        q = fourier.dft2(Hc, g.alpha, shape=(m, n), shift=(-g.offset[0], -g.offset[1]),
+                         offset=(-g.shift[0], -g.shift[1]), unitary=True, precision=g.precision)
+        grad = torch.zeros_like(opd)
+        _lib.call('lgb_phasor_adjoint', q.data_ptr(), f.data_ptr(), m, n, g.wavelength,
+                  grad.data_ptr(), g.plane[1], r0, c0, dv.stream_ptr())
+        return grad, None, None
+
+
+def mft_intensity(opd, amp, g):
+    """Differentiable PSF intensity of ``amp * exp(2 pi i opd / lambda)``."""
+    return MFTIntensity.apply(opd, amp, g)
+
+
+class PhaseRetrieval:
+    """Focus-diverse phase-retrieval loss sum_k sum (PSF_k - target_k)^2 over
+    OPD = basis . coeffs (+ an optional free-form map), with the diversity
+    OPD maps added per image."""
+
+    def __init__(self, amp, basis, diversity, targets, g):
+        dev = dv.device()
+        self.amp = dv.to_device(amp, torch.float64)
+        self.basis = dv.to_device(basis, torch.float64)          # (K, H, W)
+        self.diversity = [dv.to_device(d, torch.float64) for d in diversity]
+        self.targets = [dv.to_device(t, torch.float64) for t in targets]
+        self.g = g
+        self.device = dev
+
+    def opd(self, coeffs, free=None):
+        o = torch.einsum('k,khw->hw', coeffs, self.basis)
+        return o if free is None else o + free
+
+    def loss(self, coeffs, free=None):
+        o = self.opd(coeffs, free)
+        total = 0.0
+        for d, t in zip(self.diversity, self.targets):
+            total = total + ((mft_intensity(o + d, self.amp, self.g) - t) ** 2).sum()
+        return total

@@ -346,3 +346,79 @@ extern "C" int lgb_field_multiply(const lgb_c128* a, int lda, int ar0, int ac0,
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// K7: the element-wise halves of the adjoint (no counterpart in lentil, which
+// has no gradients).  Forward I = |F|^2; given dL/dI the Wirtinger gradient
+// dL/dF* = (dL/dI) F, its conjugate feeds an MFT with swapped offset/shift
+// (the adjoint MFT), and dL/dopd = (2 pi / lambda) * 2 Im(g conj(f)).
+// ---------------------------------------------------------------------------
+namespace lgb {
+
+__global__ void abs2_kernel(const double2* __restrict__ F, double* __restrict__ I, size_t count) {
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < count;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const double2 z = F[p];
+    I[p] = z.x * z.x + z.y * z.y;
+  }
+}
+
+__global__ void intensity_adjoint_kernel(const double2* __restrict__ F, const double* __restrict__ gI,
+                                         double2* __restrict__ Hc, size_t count) {
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < count;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const double2 z = F[p];
+    const double g = gI[p];
+    Hc[p] = make_double2(g * z.x, -g * z.y);      // conj(dL/dF*) = dL/dI * conj(F)
+  }
+}
+
+// out[r0+i, c0+j] += -2 * scale * Im(q[i,j] * f[i,j]),  q = conj(g)
+__global__ void phasor_adjoint_kernel(const double2* __restrict__ q, const double2* __restrict__ f,
+                                      int m, int n, double scale, double* __restrict__ out,
+                                      int ld, int r0, int c0) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= n || i >= m) return;
+  const double2 a = q[(size_t)i * n + j], b = f[(size_t)i * n + j];
+  out[(size_t)(r0 + i) * ld + c0 + j] += -2.0 * scale * (a.x * b.y + a.y * b.x);
+}
+
+static int grid_for(size_t count) {
+  return (int)std::max<size_t>(1, std::min<size_t>(4 * (size_t)sm_count(), (count + 255) / 256));
+}
+
+}  // namespace lgb
+
+extern "C" int lgb_abs2(const lgb_c128* F, double* I, size_t count, lgb_stream stream) {
+  LGB_REQUIRE(F && I, LGB_EINVAL, "abs2: null pointer");
+  if (!count) return LGB_OK;
+  abs2_kernel<<<grid_for(count), 256, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(F),
+                                                              I, count);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+extern "C" int lgb_intensity_adjoint(const lgb_c128* F, const double* grad_I, lgb_c128* Hc,
+                                     size_t count, lgb_stream stream) {
+  LGB_REQUIRE(F && grad_I && Hc, LGB_EINVAL, "intensity_adjoint: null pointer");
+  if (!count) return LGB_OK;
+  intensity_adjoint_kernel<<<grid_for(count), 256, 0, as_stream(stream)>>>(
+      reinterpret_cast<const double2*>(F), grad_I, reinterpret_cast<double2*>(Hc), count);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+extern "C" int lgb_phasor_adjoint(const lgb_c128* q, const lgb_c128* f, int m, int n,
+                                  double wavelength, double* grad_opd, int ld, int r0, int c0,
+                                  lgb_stream stream) {
+  LGB_REQUIRE(q && f && grad_opd, LGB_EINVAL, "phasor_adjoint: null pointer");
+  LGB_REQUIRE(wavelength != 0.0, LGB_EINVAL, "phasor_adjoint: wavelength must be nonzero");
+  if (m <= 0 || n <= 0) return LGB_OK;
+  dim3 grid(cdiv(n, 128), m);
+  phasor_adjoint_kernel<<<grid, 128, 0, as_stream(stream)>>>(
+      reinterpret_cast<const double2*>(q), reinterpret_cast<const double2*>(f), m, n,
+      2.0 * M_PI / wavelength, grad_opd, ld, r0, c0);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}

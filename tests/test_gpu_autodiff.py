@@ -1,0 +1,120 @@
+"""Gradients of the MFT intensity (phase retrieval): against a complex128
+numpy reference gradient written here and against finite differences."""
+import numpy as np
+import pytest
+import torch
+
+import lentil_gb300 as lg
+from lentil_gb300 import autodiff
+from oracle import lentil_oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(npix=64, seed=0):
+    rng = np.random.default_rng(seed)
+    amp = lo.normalize_power(lg.circle((npix, npix), npix * 0.45))
+    opd = lg.zernike_compose(amp, np.r_[0, rng.normal(0, 30e-9, 14)])
+    g = autodiff.geometry(amp, 633e-9, 1.0 / npix, 10.0, 5e-6 * 4, shape=24, oversample=2)
+    target = rng.uniform(0, 1e-3, g.shape)
+    return amp, opd, g, target
+
+
+def _numpy_grad(amp, opd, g, target):
+    """dL/dopd of L = sum(|F|^2 - T)^2 in complex128 numpy."""
+    r0, c0, m, n = g.slc
+    f = amp[r0:r0 + m, c0:c0 + n] * np.exp(2j * np.pi * opd[r0:r0 + m, c0:c0 + n] / g.wavelength)
+    E1, E2 = lo.dft2_matrices(m, n, g.shape[0], g.shape[1], g.alpha[0], g.alpha[1], 0, 0,
+                              g.offset[0], g.offset[1])
+    c = np.sqrt(abs(g.alpha[0] * g.alpha[1]))
+    F = c * E1 @ f @ E2
+    I = np.abs(F) ** 2
+    G = 2 * (I - target)
+    gf = c * E1.conj().T @ (G * F) @ E2.conj().T
+    grad = np.zeros_like(opd)
+    grad[r0:r0 + m, c0:c0 + n] = (2 * np.pi / g.wavelength) * 2 * np.imag(gf * np.conj(f))
+    return np.sum((I - target) ** 2), grad
+
+
+def _gpu_loss_grad(amp, opd, g, target):
+    o = torch.as_tensor(opd, device='cuda').requires_grad_(True)
+    a = torch.as_tensor(amp, device='cuda')
+    t = torch.as_tensor(target, device='cuda')
+    L = ((autodiff.mft_intensity(o, a, g) - t) ** 2).sum()
+    L.backward()
+    return L.item(), o.grad.cpu().numpy()
+
+
+def test_forward_matches_propagate(cuda_device):
+    amp, opd, g, _ = _setup()
+    I = autodiff.mft_intensity(torch.as_tensor(opd, device='cuda'), torch.as_tensor(amp, device='cuda'), g)
+    pl = lo.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 64, focal_length=10)
+    ref = lo.propagate_dft(lo.Wavefront(633e-9) * pl, 5e-6 * 4, shape=24, oversample=2).intensity
+    assert lo.peak_normalised_error(I.cpu().numpy(), ref) < 1e-12
+
+
+def test_gradient_vs_complex128_reference(cuda_device):
+    amp, opd, g, target = _setup()
+    L_ref, grad_ref = _numpy_grad(amp, opd, g, target)
+    L, grad = _gpu_loss_grad(amp, opd, g, target)
+    assert abs(L - L_ref) <= 1e-10 * abs(L_ref)
+    assert lo.peak_normalised_error(grad, grad_ref) < 1e-10
+
+
+def test_gradient_finite_differences(cuda_device):
+    amp, opd, g, target = _setup(seed=1)
+    _, grad = _gpu_loss_grad(amp, opd, g, target)
+    rng = np.random.default_rng(5)
+    idx = np.argwhere(amp > 0)
+    eps = 1e-11
+    for r, c in idx[rng.choice(len(idx), 6, replace=False)]:
+        p, m_ = opd.copy(), opd.copy()
+        p[r, c] += eps
+        m_[r, c] -= eps
+        Lp, _ = _numpy_grad(amp, p, g, target)
+        Lm, _ = _numpy_grad(amp, m_, g, target)
+        fd = (Lp - Lm) / (2 * eps)
+        assert abs(fd - grad[r, c]) <= 1e-5 * np.max(np.abs(grad)), (r, c, fd, grad[r, c])
+
+
+@pytest.mark.parametrize('precision,tol', [('split-fp16', 1e-4), ('split-bf16', 5e-4)])
+def test_split_gradient_close_to_fp64(cuda_device, precision, tol):
+    amp, opd, g, target = _setup(npix=128, seed=2)
+    _, grad64 = _gpu_loss_grad(amp, opd, g, target)
+    _, grads = _gpu_loss_grad(amp, opd, g._replace(precision=precision), target)
+    assert lo.peak_normalised_error(grads, grad64) < tol
+
+
+def test_phase_retrieval_coefficient_gradients(cuda_device):
+    # focus-diverse loss on Zernike + segment piston/tip/tilt coefficients
+    npix = 64
+    amp = lo.normalize_power(lg.circle((npix, npix), npix * 0.45))
+    segs = lg.hex_segments(rings=1, seg_radius=8, seg_gap=1)
+    segs = np.asarray([lg.pad(s, (npix, npix)) for s in segs]) * (amp > 0)
+    basis = [lg.zernike(amp > 0, j) for j in range(2, 12)]
+    for s in segs:
+        rho, th = lg.zernike_coordinates(s)
+        basis += [lg.zernike(s, j, rho=rho, theta=th) for j in (1, 2, 3)]
+    basis = np.asarray(basis)
+    g = autodiff.geometry(amp, 633e-9, 1.0 / npix, 10.0, 5e-6 * 4, shape=24, oversample=2)
+    z4 = lg.zernike(amp > 0, 4)
+    div = [k * 633e-9 / (z4.max() - z4.min()) * z4 for k in (-1, 0, 1)]
+    rng = np.random.default_rng(3)
+    true_c = rng.normal(0, 30e-9, len(basis))
+    pr = autodiff.PhaseRetrieval(amp, basis, div, [np.zeros(g.shape)] * 3, g)
+    with torch.no_grad():
+        tgts = [autodiff.mft_intensity(pr.opd(torch.as_tensor(true_c, device='cuda')) + d, pr.amp, g)
+                for d in pr.diversity]
+    pr.targets = [t + 1e-4 * t.max() * torch.as_tensor(rng.normal(size=g.shape), device='cuda')
+                  for t in tgts]
+    c0 = torch.zeros(len(basis), dtype=torch.float64, device='cuda', requires_grad=True)
+    L = pr.loss(c0)
+    L.backward()
+    grad = c0.grad.cpu().numpy()
+    eps = 1e-12
+    for k in (0, 3, 11, 15):
+        e = torch.zeros_like(c0)
+        e[k] = eps
+        with torch.no_grad():
+            fd = (pr.loss(c0 + e) - pr.loss(c0 - e)).item() / (2 * eps)
+        assert abs(fd - grad[k]) <= 1e-5 * np.max(np.abs(grad)), (k, fd, grad[k])
