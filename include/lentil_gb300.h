@@ -217,6 +217,9 @@ size_t lgb_psf_plan_bytes(lgb_psf_plan plan);
  * out is overwritten (accumulate == 0) or added to (accumulate != 0). */
 int lgb_psf_execute(lgb_psf_plan plan, const double* amp, const double* opd,
                     const double* weights, double* out, int accumulate, lgb_stream stream);
+/* As lgb_psf_execute for the first `count` (1..batch) PSFs of the arrays. */
+int lgb_psf_execute_batch(lgb_psf_plan plan, int count, const double* amp, const double* opd,
+                          const double* weights, double* out, int accumulate, lgb_stream stream);
 /* Device-side status of the plan's last execute; waits for the stream. */
 int lgb_psf_plan_status(lgb_psf_plan plan, lgb_stream stream);
 /* Optional per-kernel timing of lgb_psf_execute: while enabled, each launch

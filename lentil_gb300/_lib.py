@@ -64,6 +64,8 @@ SIGNATURES = {
     'lgb_psf_plan_create': (c_int, [ctypes.POINTER(PsfDesc), ctypes.POINTER(c_void_p), c_void_p]),
     'lgb_psf_plan_bytes': (c_size_t, [c_void_p]),
     'lgb_psf_execute': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    'lgb_psf_execute_batch': (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_int, c_void_p]),
     'lgb_psf_plan_status': (c_int, [c_void_p, c_void_p]),
     'lgb_psf_plan_destroy': (c_int, [c_void_p]),
     'lgb_psf_plan_profile': (c_int, [c_void_p, c_int]),

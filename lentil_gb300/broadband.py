@@ -107,16 +107,17 @@ class PSFPlan:
         amp = amp if amp.dtype == torch.float64 and amp.is_contiguous() else amp.double().contiguous()
         opd = opd if opd.dtype == torch.float64 and opd.is_contiguous() else opd.double().contiguous()
         weights = dv.to_device(weights, torch.float64)
-        shp = (self.batch,) + self.plane_shape
-        if tuple(amp.shape) != shp or tuple(opd.shape) != shp:
-            raise ValueError(f'amp/opd must have shape {shp}')
-        if weights.numel() != self.batch * self.L:
-            raise ValueError(f'weights must have {self.batch * self.L} entries')
+        count = int(amp.shape[0])
+        shp = (count,) + self.plane_shape
+        if not 1 <= count <= self.batch or tuple(amp.shape) != shp or tuple(opd.shape) != shp:
+            raise ValueError(f'amp/opd must have shape (n,) + {self.plane_shape}, n <= {self.batch}')
+        if weights.numel() < count * self.L:
+            raise ValueError(f'weights must have {count * self.L} entries')
         if out is None:
-            out = torch.empty((self.batch,) + self.image_shape, dtype=torch.float64, device=dev)
+            out = torch.empty((count,) + self.image_shape, dtype=torch.float64, device=dev)
             accumulate = False
-        _lib.call('lgb_psf_execute', self._h, amp.data_ptr(), opd.data_ptr(), weights.data_ptr(),
-                  out.data_ptr(), int(bool(accumulate)), dv.stream_ptr())
+        _lib.call('lgb_psf_execute_batch', self._h, count, amp.data_ptr(), opd.data_ptr(),
+                  weights.data_ptr(), out.data_ptr(), int(bool(accumulate)), dv.stream_ptr())
         if check:
             _lib.call('lgb_psf_plan_status', self._h, dv.stream_ptr())
         return out

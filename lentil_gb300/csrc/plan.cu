@@ -365,11 +365,12 @@ extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan,
 
 extern "C" size_t lgb_psf_plan_bytes(lgb_psf_plan plan) { return plan ? plan->bytes : 0; }
 
-extern "C" int lgb_psf_execute(lgb_psf_plan P, const double* amp, const double* opd,
-                               const double* weights, double* out, int accumulate, lgb_stream stream) {
+static int psf_execute_n(lgb_psf_plan P, int B, const double* amp, const double* opd,
+                         const double* weights, double* out, int accumulate, lgb_stream stream) {
   LGB_REQUIRE(P && amp && opd && out, LGB_EINVAL, "psf_execute: null argument");
   const lgb_psf_desc& d = P->d;
-  const int L = d.n_wavelengths, B = d.batch;
+  LGB_REQUIRE(B >= 1 && B <= d.batch, LGB_EINVAL, "psf_execute: count outside 1..batch");
+  const int L = d.n_wavelengths;
   cudaStream_t s = as_stream(stream);
   int st;
   const size_t img = (size_t)d.out_rows * d.out_cols;
@@ -445,6 +446,18 @@ extern "C" int lgb_psf_execute(lgb_psf_plan P, const double* amp, const double* 
                                         (long long)img, d.win_r0, d.win_c0, B, s)))
     return st;
   return prof_end(P, LGB_PROFILE_OTHER, s, ev);
+}
+
+extern "C" int lgb_psf_execute(lgb_psf_plan P, const double* amp, const double* opd,
+                               const double* weights, double* out, int accumulate, lgb_stream stream) {
+  LGB_REQUIRE(P, LGB_EINVAL, "psf_execute: null plan");
+  return psf_execute_n(P, P->d.batch, amp, opd, weights, out, accumulate, stream);
+}
+
+extern "C" int lgb_psf_execute_batch(lgb_psf_plan P, int count, const double* amp,
+                                     const double* opd, const double* weights, double* out,
+                                     int accumulate, lgb_stream stream) {
+  return psf_execute_n(P, count, amp, opd, weights, out, accumulate, stream);
 }
 
 extern "C" int lgb_psf_plan_profile(lgb_psf_plan P, int enable) {

@@ -1,0 +1,85 @@
+"""Continuous-batching server: every result equals the same PSF computed
+alone (fused plan and oracle) while requests of different sizes overlap."""
+import numpy as np
+import pytest
+
+import lentil_gb300 as lg
+from lentil_gb300 import serving
+from oracle import lentil_oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-6    # split-precision PSF vs its own result computed alone / the oracle
+
+
+def _request(rng, npix, det, L, segmented=False):
+    if segmented:
+        segs = lg.hex_segments(rings=2, seg_radius=npix * 0.114, seg_gap=1)
+        amp = lg.pad(np.sum(segs, axis=0), (npix, npix))
+    else:
+        amp = lg.circle((npix, npix), npix * 0.45)
+    amp = lg.normalize_power(amp)
+    opd = lg.zernike_compose(amp > 0, np.r_[0, rng.normal(0, 20e-9, 10)])
+    wl = np.linspace(400e-9, 1000e-9, L) if L > 1 else np.array([700e-9])
+    w = rng.uniform(0.5, 1.5, L)
+    return serving.PSFRequest(amp, opd, wl, w / w.sum(), 1.0 / npix, 10.0, 5e-6 * 256 / npix,
+                              det, oversample=2)
+
+
+def _alone(req):
+    pl = lo.Pupil(amplitude=req.amp, opd=req.opd, pixelscale=req.pixelscale_in,
+                  focal_length=req.focal_length)
+    return lo.broadband_psf(pl, req.wavelengths, req.weights, req.det_pixelscale,
+                            shape=req.det_shape, oversample=req.oversample)
+
+
+def test_results_same_alone_and_in_mix(cuda_device):
+    rng = np.random.default_rng(7)
+    reqs = [_request(rng, npix, det, L, seg) for npix, det, L, seg in
+            [(64, 16, 3, False), (96, 24, 5, True), (64, 16, 3, False), (128, 32, 2, False),
+             (64, 16, 3, False), (96, 24, 5, True), (128, 20, 1, True), (64, 16, 3, False)]]
+    with serving.PSFServer(streams=3, max_batch=2, precision='split') as srv:
+        futs = [srv.submit(r) for r in reqs]
+        results = [f.result(timeout=120) for f in futs]
+        stats = dict(srv.stats)
+    assert stats['completed'] == len(reqs)
+    assert stats['batched'] == len(reqs)
+    assert stats['launches'] < len(reqs)          # same-plan requests were batched
+    for r, img in zip(reqs, results):
+        ref = _alone(r)
+        assert img.shape == ref.shape
+        assert lo.peak_normalised_error(img, ref) < TOL
+    # alone through a fresh server (no mix) gives the same image within tolerance
+    with serving.PSFServer(streams=1, max_batch=1, precision='split') as srv:
+        solo = [srv.submit(r).result(timeout=120) for r in reqs[:3]]
+    for a, b in zip(solo, results[:3]):
+        assert lo.peak_normalised_error(a, b) < TOL
+
+
+def test_budget_rejects_oversize_and_cancel(cuda_device):
+    rng = np.random.default_rng(8)
+    with serving.PSFServer(hbm_budget=64 << 20, streams=1, max_batch=1) as srv:
+        big = _request(rng, 512, 256, 64)            # needs far more than 64 MB
+        f = srv.submit(big)
+        with pytest.raises(MemoryError):
+            f.result(timeout=120)
+        small = _request(rng, 64, 16, 2)
+        assert lo.peak_normalised_error(srv.submit(small).result(timeout=120), _alone(small)) < TOL
+    with serving.PSFServer(streams=1, max_batch=1) as srv:
+        reqs = [_request(rng, 64, 16, 2) for _ in range(4)]
+        futs = [srv.submit(r) for r in reqs]
+        srv.cancel(reqs[-1])
+        for f in futs[:-1]:
+            f.result(timeout=120)
+        assert futs[-1].cancelled() or futs[-1].done()
+
+
+def test_eviction_under_budget(cuda_device):
+    rng = np.random.default_rng(9)
+    reqs = [_request(rng, 64, 16, L) for L in (2, 3, 4, 5, 6)]
+    one = serving.plan_bytes_estimate((64, 64), (0, 0, 58, 58), (32, 32), 6, 1, 'split')
+    with serving.PSFServer(hbm_budget=int(2.5 * one), streams=1, max_batch=1) as srv:
+        out = [srv.submit(r).result(timeout=120) for r in reqs]
+        assert srv.stats['evicted'] >= 1
+    for r, img in zip(reqs, out):
+        assert lo.peak_normalised_error(img, _alone(r)) < TOL
