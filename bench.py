@@ -42,7 +42,7 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--batch', type=int, default=1, help='PSFs per step')
-    ap.add_argument('--precision', default='split-fp16',
+    ap.add_argument('--precision', default='split-bf16',
                     choices=['split-fp16', 'split-bf16', 'fp64'])
     ap.add_argument('--fp64-steps', type=int, default=2,
                     help='timed steps of the plain complex128 plan (0 to skip)')
@@ -50,8 +50,11 @@ def parse():
                     help='wavelengths in the bounded CPU-baseline sample')
     ap.add_argument('--npix', type=int, default=1024)
     ap.add_argument('--wavelengths', type=int, default=64)
+    ap.add_argument('--rates', default='10,50,200,1000',
+                    help='serving: Poisson arrival rates (requests/s)')
+    ap.add_argument('--duration', type=float, default=2.0, help='serving: seconds per rate')
     ap.add_argument('--workload', default='broadband',
-                    choices=['broadband', 'monochromatic', 'phase_retrieval'],
+                    choices=['broadband', 'monochromatic', 'phase_retrieval', 'serving'],
                     help='broadband: the headline workload; the others measure the '
                          'monochromatic 256^2 PSF and the focus-diverse gradient')
     return ap.parse_args()
@@ -502,8 +505,75 @@ def run_phase_retrieval(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(args):
+    """Poisson stream of PSF requests: pupil 256/512/1024/2048, detector
+    64..1024 at oversample 2, 1-128 wavelengths over 400-1000 nm, circular or
+    18-hex amplitude, Noll 2-11 N(0,20nm) OPD; continuous batching server."""
+    import lentil_gb300 as lg
+    from lentil_gb300 import serving
+    rng = np.random.default_rng(3)
+    pupils = {}
+    for npix in (256, 512, 1024, 2048):
+        circ = lg.normalize_power(lg.circle((npix, npix), npix // 2))
+        segs = lg.hex_segments(rings=2, seg_radius=116.8 * npix / 1024, seg_gap=2)
+        hexa = lg.normalize_power(lg.pad(np.sum(segs, axis=0), (npix, npix)))
+        opds = []
+        rho, th = lg.zernike_coordinates(circ > 0)
+        basis = np.asarray([lg.zernike(circ > 0, j, rho=rho, theta=th) for j in range(2, 12)])
+        for _ in range(3):
+            c = rng.normal(0, 20e-9, 10)
+            opds.append(np.tensordot(c, basis, 1))
+        pupils[npix] = (circ, hexa, opds)
+
+    def make_request():
+        npix = int(rng.choice([256, 512, 1024, 2048]))
+        det = int(rng.choice([64, 128, 256, 512, 1024]))
+        L = int(rng.integers(1, 129))
+        circ, hexa, opds = pupils[npix]
+        amp = circ if rng.random() < 0.5 else hexa
+        wl = np.linspace(400e-9, 1000e-9, L) if L > 1 else np.array([700e-9])
+        return serving.PSFRequest(amp, opds[rng.integers(len(opds))], wl, np.full(L, 1.0 / L),
+                                  1.0 / npix, 10.0, 5e-6 * 1024 / npix, det, oversample=2)
+
+    results = []
+    with serving.PSFServer(streams=4, max_batch=4, precision=args.precision) as srv:
+        for rate in [float(r) for r in args.rates.split(',')]:
+            reqs = []
+            t0 = time.perf_counter()
+            t_next = t0
+            while t_next - t0 < args.duration:
+                now = time.perf_counter()
+                if now < t_next:
+                    time.sleep(min(t_next - now, 0.002))
+                    continue
+                r = make_request()
+                srv.submit(r)
+                reqs.append(r)
+                t_next += rng.exponential(1.0 / rate)
+            for r in reqs:
+                r.future.result()
+            t_end = max(r.t_done for r in reqs)
+            lat = sorted(1e3 * r.latency for r in reqs)
+            results.append({'rate_per_s': rate, 'requests': len(reqs),
+                            'throughput_psfs_per_s': len(reqs) / (t_end - t0),
+                            'p50_ms': float(np.percentile(lat, 50)),
+                            'p99_ms': float(np.percentile(lat, 99))})
+        stats = dict(srv.stats)
+    best = max(x['throughput_psfs_per_s'] for x in results)
+    line = {'metric': 'serving mix PSFs/s with p50/p99 latency', 'value': best, 'unit': 'PSFs/s',
+            'n_gpus': 1, 'higher_is_better': True, 'dtype': args.precision,
+            'data': 'synthetic (seeded)', 'sweep': results, 'server_stats': stats,
+            'config': {'workload': 'Poisson PSF requests: pupil 256/512/1024/2048, detector '
+                                   '64-1024 x oversample 2, 1-128 wavelengths 400-1000 nm, circular '
+                                   'or 18-hex amplitude, Noll 2-11 N(0,20nm)',
+                       'streams': 4, 'max_batch': 4, 'duration_s_per_rate': args.duration}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == 'serving':
+        return run_serving(args)
     if args.impl == 'reference':
         run_reference(args)
     elif args.workload == 'monochromatic':

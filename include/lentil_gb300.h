@@ -233,6 +233,8 @@ int lgb_psf_plan_status(lgb_psf_plan plan, lgb_stream stream);
 #define LGB_PROFILE_SLOTS 4
 int lgb_psf_plan_profile(lgb_psf_plan plan, int enable);
 int lgb_psf_plan_kernel_times(lgb_psf_plan plan, double* ms, int* launches, int n);
+/* Releases the plan's memory (stream-ordered on the creation stream); call
+ * it after the plan's last execute has completed. */
 int lgb_psf_plan_destroy(lgb_psf_plan plan);
 
 #ifdef __cplusplus

@@ -17,7 +17,7 @@
 // every MMA, a bias that grows with the length of the accumulation chain
 // (measured: 1.8e-5 relative at K = 2048).  So the dominant hi.hi products
 // are accumulated in short chains: TMEM region X is restarted every KSUB
-// k-steps and the epilogue warps fold each chunk into round-to-nearest FP32
+// (= 4, one 64-wide K block) k-steps and the epilogue warps fold each chunk into round-to-nearest FP32
 // registers, while the MMA issues the small cross terms into region Y (one
 // long chain; its truncation is 2^-8 smaller).  The epilogue drain of X
 // hides behind the Y instructions.
@@ -46,7 +46,7 @@ namespace tc {
 constexpr int BM = 128, BN = 256, BK = 64, STAGES = 2;
 constexpr int KSTEPS = BK / 16;                            // MMA k-steps per K block
 #ifndef LGB_KSUB
-#define LGB_KSUB 2
+#define LGB_KSUB 4
 #endif
 constexpr int KSUB = LGB_KSUB;                             // k-steps per hi.hi chain
 constexpr int CHUNKS = KSTEPS / KSUB;                      // X chunks per K block

@@ -212,6 +212,7 @@ struct lgb_psf_plan_s {
   std::vector<double> lam, ar, ac, sr, sc;
   void* mem = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;   // creation stream: the plan's memory is freed on it
   int kp1 = 0, kp2 = 0;
   // device views
   int* err = nullptr;
@@ -314,6 +315,7 @@ extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan,
   P->kp2 = round_up(d.n, 32);
   P->bytes = plan_carve(P, nullptr);
   cudaStream_t s = as_stream(stream);
+  P->stream = s;
   cudaError_t e = cudaMallocAsync(&P->mem, P->bytes, s);
   if (e != cudaSuccess) {
     delete P;
@@ -498,7 +500,9 @@ extern "C" int lgb_psf_plan_status(lgb_psf_plan P, lgb_stream stream) {
 
 extern "C" int lgb_psf_plan_destroy(lgb_psf_plan P) {
   if (!P) return LGB_OK;
-  cudaError_t e = cudaFree(P->mem);
+  // stream-ordered free: no device-wide synchronisation; the caller destroys
+  // a plan only after the work that used it has completed
+  cudaError_t e = cudaFreeAsync(P->mem, P->stream);
   delete P;
   if (e != cudaSuccess) return check_cuda(e, "cudaFree(psf plan)");
   return LGB_OK;
