@@ -531,12 +531,16 @@ def run_serving(args):
         L = int(rng.integers(1, 129))
         circ, hexa, opds = pupils[npix]
         amp = circ if rng.random() < 0.5 else hexa
-        wl = np.linspace(400e-9, 1000e-9, L) if L > 1 else np.array([700e-9])
-        return serving.PSFRequest(amp, opds[rng.integers(len(opds))], wl, np.full(L, 1.0 / L),
-                                  1.0 / npix, 10.0, 5e-6 * 1024 / npix, det, oversample=2)
+        # L wavelengths spread over the server's 128-point 400-1000 nm grid
+        idx = np.unique(np.linspace(0, 127, L).round().astype(int))
+        wl = grid[idx]
+        return serving.PSFRequest(amp, opds[rng.integers(len(opds))], wl,
+                                  np.full(len(wl), 1.0 / len(wl)), 1.0 / npix, 10.0,
+                                  5e-6 * 1024 / npix, det, oversample=2)
 
+    grid = np.linspace(400e-9, 1000e-9, 128)
     results = []
-    with serving.PSFServer(streams=4, max_batch=4, precision=args.precision) as srv:
+    with serving.PSFServer(streams=4, max_batch=4, precision=args.precision, grid=grid) as srv:
         for rate in [float(r) for r in args.rates.split(',')]:
             reqs = []
             t0 = time.perf_counter()
@@ -564,7 +568,8 @@ def run_serving(args):
             'n_gpus': 1, 'higher_is_better': True, 'dtype': args.precision,
             'data': 'synthetic (seeded)', 'sweep': results, 'server_stats': stats,
             'config': {'workload': 'Poisson PSF requests: pupil 256/512/1024/2048, detector '
-                                   '64-1024 x oversample 2, 1-128 wavelengths 400-1000 nm, circular '
+                                   '64-1024 x oversample 2, 1-128 wavelengths on a 128-point '
+                                   '400-1000 nm grid, circular '
                                    'or 18-hex amplitude, Noll 2-11 N(0,20nm)',
                        'streams': 4, 'max_batch': 4, 'duration_s_per_rate': args.duration}}
     print(json.dumps(line), flush=True)

@@ -205,7 +205,7 @@ typedef struct {
   const double* alpha_c;      /* host [L] */
   const double* shift_r;      /* host [L], output-pixel shift of the DC */
   const double* shift_c;      /* host [L] */
-  int batch;                  /* PSFs per execute */
+  int batch;                  /* PSFs per execute (0: matrices only, see lgb_psf_execute_ws) */
   int precision;              /* LGB_FP64 / LGB_SPLIT_BF16 / LGB_SPLIT_FP16 */
 } lgb_psf_desc;
 
@@ -220,6 +220,25 @@ int lgb_psf_execute(lgb_psf_plan plan, const double* amp, const double* opd,
 /* As lgb_psf_execute for the first `count` (1..batch) PSFs of the arrays. */
 int lgb_psf_execute_batch(lgb_psf_plan plan, int count, const double* amp, const double* opd,
                           const double* weights, double* out, int accumulate, lgb_stream stream);
+/* As lgb_psf_execute_batch over a subset of the plan's wavelengths:
+ * lam_idx (device int32 [n_sel]) picks the plan wavelengths used; weights is
+ * [count][n_sel].  The plan's DFT matrices serve every subset, so a plan
+ * built on a spectral grid is a device-resident DFT-matrix cache for
+ * requests with any wavelengths of that grid.  Split-precision plans only. */
+int lgb_psf_execute_subset(lgb_psf_plan plan, int count, const int* lam_idx, int n_sel,
+                           const double* amp, const double* opd, const double* weights,
+                           double* out, int accumulate, lgb_stream stream);
+/* Caller-workspace execute: a plan created with batch == 0 holds only its
+ * DFT matrices; every execute then takes its per-launch operands (f^T, G,
+ * intensity window, status word) from `workspace`
+ * (lgb_psf_execute_workspace_size(plan, count, n_sel) bytes, 256-byte
+ * aligned), so one plan may run on several streams at once.  lam_idx may be
+ * NULL (all wavelengths; n_sel ignored).  lgb_dft2_status(workspace, stream)
+ * reports the device status of the launch.  Split-precision plans only. */
+size_t lgb_psf_execute_workspace_size(lgb_psf_plan plan, int count, int n_sel);
+int lgb_psf_execute_ws(lgb_psf_plan plan, int count, const int* lam_idx, int n_sel,
+                       const double* amp, const double* opd, const double* weights, double* out,
+                       int accumulate, void* workspace, size_t workspace_bytes, lgb_stream stream);
 /* Device-side status of the plan's last execute; waits for the stream. */
 int lgb_psf_plan_status(lgb_psf_plan plan, lgb_stream stream);
 /* Optional per-kernel timing of lgb_psf_execute: while enabled, each launch

@@ -66,6 +66,11 @@ SIGNATURES = {
     'lgb_psf_execute': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     'lgb_psf_execute_batch': (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_int, c_void_p]),
+    'lgb_psf_execute_subset': (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p,
+                                       c_void_p, c_void_p, c_int, c_void_p]),
+    'lgb_psf_execute_workspace_size': (c_size_t, [c_void_p, c_int, c_int]),
+    'lgb_psf_execute_ws': (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_int, c_void_p, c_size_t, c_void_p]),
     'lgb_psf_plan_status': (c_int, [c_void_p, c_void_p]),
     'lgb_psf_plan_destroy': (c_int, [c_void_p]),
     'lgb_psf_plan_profile': (c_int, [c_void_p, c_int]),

@@ -100,24 +100,51 @@ class PSFPlan:
                 pass
             self._h = None
 
-    def execute(self, amp, opd, weights, out=None, accumulate=False, check=True):
-        """amp (mask applied), opd: [batch, H, W] float64 CUDA tensors;
-        weights: [batch, L]; returns out [batch, rows, cols] float64."""
+    def workspace_bytes(self, count, n_sel=None):
+        """Bytes of a caller workspace for ``execute(..., workspace=...)``."""
+        return _lib.load().lgb_psf_execute_workspace_size(self._h, count,
+                                                          self.L if n_sel is None else n_sel)
+
+    def execute(self, amp, opd, weights, out=None, accumulate=False, check=True, lam_idx=None,
+                workspace=None):
+        """amp (mask applied), opd: [n, H, W] float64 CUDA tensors (n <= batch);
+        weights: [n, L] (or [n, len(lam_idx)]); returns out [n, rows, cols]
+        float64.  ``lam_idx`` (int32 CUDA tensor) restricts the PSFs to those
+        of the plan's wavelengths."""
         dev = dv.device()
         amp = amp if amp.dtype == torch.float64 and amp.is_contiguous() else amp.double().contiguous()
         opd = opd if opd.dtype == torch.float64 and opd.is_contiguous() else opd.double().contiguous()
         weights = dv.to_device(weights, torch.float64)
         count = int(amp.shape[0])
         shp = (count,) + self.plane_shape
-        if not 1 <= count <= self.batch or tuple(amp.shape) != shp or tuple(opd.shape) != shp:
-            raise ValueError(f'amp/opd must have shape (n,) + {self.plane_shape}, n <= {self.batch}')
-        if weights.numel() < count * self.L:
-            raise ValueError(f'weights must have {count * self.L} entries')
+        cap = self.batch if workspace is None else count
+        if not 1 <= count <= cap or tuple(amp.shape) != shp or tuple(opd.shape) != shp:
+            raise ValueError(f'amp/opd must have shape (n,) + {self.plane_shape}, n <= {cap}')
+        n_sel = self.L if lam_idx is None else int(lam_idx.numel())
+        if weights.numel() < count * n_sel:
+            raise ValueError(f'weights must have {count * n_sel} entries')
         if out is None:
             out = torch.empty((count,) + self.image_shape, dtype=torch.float64, device=dev)
             accumulate = False
-        _lib.call('lgb_psf_execute_batch', self._h, count, amp.data_ptr(), opd.data_ptr(),
-                  weights.data_ptr(), out.data_ptr(), int(bool(accumulate)), dv.stream_ptr())
+        if workspace is not None:
+            if lam_idx is not None and (lam_idx.dtype != torch.int32 or not lam_idx.is_cuda):
+                raise TypeError('lam_idx must be an int32 CUDA tensor')
+            _lib.call('lgb_psf_execute_ws', self._h, count, dv.ptr(lam_idx), n_sel,
+                      amp.data_ptr(), opd.data_ptr(), weights.data_ptr(), out.data_ptr(),
+                      int(bool(accumulate)), workspace.data_ptr(), workspace.numel(),
+                      dv.stream_ptr())
+            if check:
+                _lib.call('lgb_dft2_status', workspace.data_ptr(), dv.stream_ptr())
+            return out
+        if lam_idx is None:
+            _lib.call('lgb_psf_execute_batch', self._h, count, amp.data_ptr(), opd.data_ptr(),
+                      weights.data_ptr(), out.data_ptr(), int(bool(accumulate)), dv.stream_ptr())
+        else:
+            if lam_idx.dtype != torch.int32 or not lam_idx.is_cuda:
+                raise TypeError('lam_idx must be an int32 CUDA tensor')
+            _lib.call('lgb_psf_execute_subset', self._h, count, lam_idx.data_ptr(), n_sel,
+                      amp.data_ptr(), opd.data_ptr(), weights.data_ptr(), out.data_ptr(),
+                      int(bool(accumulate)), dv.stream_ptr())
         if check:
             _lib.call('lgb_psf_plan_status', self._h, dv.stream_ptr())
         return out

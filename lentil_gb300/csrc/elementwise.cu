@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a) {
   const int L = PHASOR ? a.L : 1;
   for (int l = 0; l < L; ++l) {
     if (PHASOR) {
-      const float2 kk = a.khalf[l];                  // 2/lambda as a float-float pair
+      const float2 kk = a.khalf[a.lam_idx ? a.lam_idx[l] : l];   // 2/lambda, float-float pair
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         // x = opd * 2/lambda half-cycles, reduced mod 2 before sincospi

@@ -38,6 +38,7 @@ struct SplitFieldArgs {
   const float* maxabs;     // [batch] max |component| of the field (device)
   uint16_t* hi;            // [batch*L][n][2*kp]
   uint16_t* lo;
+  const int* lam_idx;      // optional [L] device: wavelength -> khalf slot
 };
 int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s);
 
@@ -86,6 +87,8 @@ struct SplitMftProblem {
   double complex_scale;    // complex epilogue: extra scale (unitary factor)
   int* err;                // device error flag
   cudaEvent_t* events;     // optional [4]: recorded around the stage-1 and stage-2 launches
+  const int* lam_idx;      // optional [L] device: wavelength -> DFT-matrix slot
+  int L_bank;              // DFT-matrix slots held (when lam_idx is set)
 };
 int launch_split_mft(const SplitMftProblem& p, cudaStream_t s);
 // scale applied to the stage-1 result before its 16-bit split

@@ -82,7 +82,12 @@ struct Params {
   double* out;               // stage 2 complex: [M][N] complex128
   double cscale;
   int* err;
+  const int* lam_idx;        // [L] wavelength -> DFT-matrix slot, or null (identity)
 };
+
+__device__ __forceinline__ int matrix_slot(const Params& p, int lam) {
+  return p.lam_idx ? p.lam_idx[lam] : lam;
+}
 
 // ------------------------------------------------------------------ PTX ---
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -264,7 +269,7 @@ __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int
   if (p.epilogue == 0) {
     const float inv = 1.f / (sf * p.sG);
     const double wt = p.weights ? p.weights[(size_t)w.psf * p.L + w.lam] : 1.0;
-    const float coef = (float)(wt * p.unit2[w.lam]) * inv * inv;
+    const float coef = (float)(wt * p.unit2[matrix_slot(p, w.lam)]) * inv * inv;
     float* dst = p.wbuf + ((size_t)w.psf * p.M + u) * p.ldw + v0;
 #pragma unroll
     for (int j = 0; j < 64; j += 4) {
@@ -339,8 +344,8 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
       for (int i = blockIdx.x; ok && i < p.n_items; i += gridDim.x) {
         const Item w = decode(p, i);
         // stage 1: A = E1 block of lam, B = f^T of q; stage 2: A = G of q, B = E2 block of lam
-        const int az = p.stage == 1 ? w.lam : w.q;
-        const int bz = p.stage == 1 ? w.q : w.lam;
+        const int az = p.stage == 1 ? matrix_slot(p, w.lam) : w.q;
+        const int bz = p.stage == 1 ? w.q : matrix_slot(p, w.lam);
         for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
           const int s = it % STAGES;
           if (!mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1, p.err)) { ok = false; break; }
@@ -530,8 +535,9 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   int st;
 
   // ---- stage 1: G = E1 . f
-  if ((st = make_map(&a_hi, q.e1_hi, q.bf16, 2 * q.kp1, mrows1, q.L, BM))) return st;
-  if ((st = make_map(&a_lo, q.e1_lo, q.bf16, 2 * q.kp1, mrows1, q.L, BM))) return st;
+  const int Lm = q.lam_idx ? q.L_bank : q.L;     // DFT-matrix slots held
+  if ((st = make_map(&a_hi, q.e1_hi, q.bf16, 2 * q.kp1, mrows1, Lm, BM))) return st;
+  if ((st = make_map(&a_lo, q.e1_lo, q.bf16, 2 * q.kp1, mrows1, Lm, BM))) return st;
   if ((st = make_map(&b_hi, q.f_hi, q.bf16, 2 * q.kp1, q.n, Q, BN))) return st;
   if ((st = make_map(&b_lo, q.f_lo, q.bf16, 2 * q.kp1, q.n, Q, BN))) return st;
   Params p{};
@@ -548,6 +554,7 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   p.g_hi = q.g_hi; p.g_lo = q.g_lo;
   p.maxabs = q.maxabs;
   p.err = q.err;
+  p.lam_idx = q.lam_idx;
   if (q.events) LGB_CUDA(cudaEventRecord(q.events[0], s));
   st = q.bf16 ? launch_one<true>(p, a_hi, a_lo, b_hi, b_lo, s)
               : launch_one<false>(p, a_hi, a_lo, b_hi, b_lo, s);
@@ -557,8 +564,8 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   // ---- stage 2: F = G . E2 (+ epilogue)
   if ((st = make_map(&a_hi, q.g_hi, q.bf16, 2 * q.kp2, q.M, Q, BM))) return st;
   if ((st = make_map(&a_lo, q.g_lo, q.bf16, 2 * q.kp2, q.M, Q, BM))) return st;
-  if ((st = make_map(&b_hi, q.e2_hi, q.bf16, 2 * q.kp2, nrows2, q.L, BN))) return st;
-  if ((st = make_map(&b_lo, q.e2_lo, q.bf16, 2 * q.kp2, nrows2, q.L, BN))) return st;
+  if ((st = make_map(&b_hi, q.e2_hi, q.bf16, 2 * q.kp2, nrows2, Lm, BN))) return st;
+  if ((st = make_map(&b_lo, q.e2_lo, q.bf16, 2 * q.kp2, nrows2, Lm, BN))) return st;
   p.stage = 2;
   p.kblocks = 2 * q.kp2 / BK;
   p.m_tiles = cdiv(q.M, BM);

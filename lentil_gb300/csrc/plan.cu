@@ -207,6 +207,33 @@ extern "C" size_t lgb_idft2_workspace_size(int m, int n, int M, int N, int preci
 // ===========================================================================
 // broadband PSF plan
 // ===========================================================================
+// Per-execute operands of the split path: the phasor operand f^T, the
+// stage-1 result G, the FP32 intensity window, the per-PSF field maxima and
+// the device status word (first, so a workspace's status is at offset 0).
+struct SplitOperands {
+  int* err = nullptr;
+  float* maxabs = nullptr;
+  uint16_t *fh = nullptr, *fl = nullptr, *gh = nullptr, *gl = nullptr;
+  float* wbuf = nullptr;
+  int ldw = 0;
+};
+
+static size_t carve_operands(void* base, const lgb_psf_desc& d, int kp1, int kp2, int B, int L,
+                             SplitOperands* o) {
+  Carve c(base);
+  SplitOperands t;
+  const size_t Q = (size_t)B * L;
+  t.err = c.take<int>(4);
+  t.maxabs = c.take<float>(B);
+  t.fh = c.take<uint16_t>(Q * d.n * 2 * kp1);
+  t.fl = c.take<uint16_t>(Q * d.n * 2 * kp1);
+  t.gh = c.take<uint16_t>(Q * d.M * 2 * kp2);
+  t.gl = c.take<uint16_t>(Q * d.M * 2 * kp2);
+  t.ldw = round_up(d.N, 4);
+  t.wbuf = c.take<float>((size_t)B * d.M * t.ldw);
+  if (o) *o = t;
+  return c.used;
+}
 struct lgb_psf_plan_s {
   lgb_psf_desc d;
   std::vector<double> lam, ar, ac, sr, sc;
@@ -223,9 +250,7 @@ struct lgb_psf_plan_s {
   float* maxabs = nullptr;         // [batch]
   // split
   uint16_t *e1h = nullptr, *e1l = nullptr, *e2h = nullptr, *e2l = nullptr;
-  uint16_t *fh = nullptr, *fl = nullptr, *gh = nullptr, *gl = nullptr;
-  float* wbuf = nullptr;           // [batch][M][ldw] FP32 intensity window
-  int ldw = 0;
+  SplitOperands ops;               // plan-owned operands (batch > 0)
   // optional per-kernel timing: event pairs recorded around each launch
   bool profile = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -252,12 +277,15 @@ static size_t plan_carve(lgb_psf_plan_s* P, void* base) {
     P->e1l = c.take<uint16_t>(L * mrows1 * 2 * P->kp1);
     P->e2h = c.take<uint16_t>(L * nrows2 * 2 * P->kp2);
     P->e2l = c.take<uint16_t>(L * nrows2 * 2 * P->kp2);
-    P->fh = c.take<uint16_t>(Q * d.n * 2 * P->kp1);
-    P->fl = c.take<uint16_t>(Q * d.n * 2 * P->kp1);
-    P->gh = c.take<uint16_t>(Q * d.M * 2 * P->kp2);
-    P->gl = c.take<uint16_t>(Q * d.M * 2 * P->kp2);
-    P->ldw = round_up(d.N, 4);
-    P->wbuf = c.take<float>((size_t)B * d.M * P->ldw);
+    (void)Q;
+    if (B > 0) {
+      c.used = align_up(c.used, 256);
+      const size_t sz = carve_operands(base ? static_cast<char*>(base) + c.used : nullptr, d,
+                                       P->kp1, P->kp2, B, L, &P->ops);
+      if (!base) P->ops = SplitOperands();
+      c.used += sz;
+      P->ops.err = P->err;
+    }
   } else {
     const size_t Q = (size_t)B * L;
     P->E1 = c.take<double2>((size_t)L * d.M * d.m);
@@ -299,7 +327,9 @@ extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan,
   LGB_REQUIRE(d.n_wavelengths > 0 && d.wavelengths && d.alpha_r && d.alpha_c && d.shift_r &&
                   d.shift_c,
               LGB_EINVAL, "psf_plan_create: wavelength arrays required");
-  LGB_REQUIRE(d.batch > 0, LGB_EINVAL, "psf_plan_create: batch must be positive");
+  LGB_REQUIRE(d.batch > 0 || (d.batch == 0 && (d.precision == LGB_SPLIT_BF16 ||
+                                                d.precision == LGB_SPLIT_FP16)),
+              LGB_EINVAL, "psf_plan_create: batch must be positive (0: split matrices only)");
   LGB_REQUIRE(d.precision == LGB_FP64 || is_split(d.precision), LGB_EINVAL,
               "psf_plan_create: unknown precision");
   const int L = d.n_wavelengths;
@@ -367,44 +397,55 @@ extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan,
 
 extern "C" size_t lgb_psf_plan_bytes(lgb_psf_plan plan) { return plan ? plan->bytes : 0; }
 
-static int psf_execute_n(lgb_psf_plan P, int B, const double* amp, const double* opd,
-                         const double* weights, double* out, int accumulate, lgb_stream stream) {
+static int psf_execute_n(lgb_psf_plan P, int B, const int* lam_idx, int n_sel, const double* amp,
+                         const double* opd, const double* weights, double* out, int accumulate,
+                         lgb_stream stream, const SplitOperands* ops_in = nullptr) {
   LGB_REQUIRE(P && amp && opd && out, LGB_EINVAL, "psf_execute: null argument");
   const lgb_psf_desc& d = P->d;
-  LGB_REQUIRE(B >= 1 && B <= d.batch, LGB_EINVAL, "psf_execute: count outside 1..batch");
-  const int L = d.n_wavelengths;
+  LGB_REQUIRE(B >= 1 && (ops_in || B <= d.batch), LGB_EINVAL,
+              "psf_execute: count outside 1..batch");
+  const SplitOperands& ops = ops_in ? *ops_in : P->ops;
+  int* const errp = ops_in ? ops_in->err : P->err;
+  LGB_REQUIRE(!lam_idx || (n_sel >= 1 && n_sel <= d.n_wavelengths), LGB_EINVAL,
+              "psf_execute: wavelength subset size outside 1..n_wavelengths");
+  LGB_REQUIRE(!lam_idx || is_split(d.precision), LGB_EUNSUPPORTED,
+              "psf_execute: wavelength subsets need a split-precision plan");
+  const int L = lam_idx ? n_sel : d.n_wavelengths;
   cudaStream_t s = as_stream(stream);
   int st;
   const size_t img = (size_t)d.out_rows * d.out_cols;
   if (!accumulate) LGB_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * img * B, s));
-  LGB_CUDA(cudaMemsetAsync(P->err, 0, sizeof(int), s));
+  LGB_CUDA(cudaMemsetAsync(errp, 0, sizeof(int), s));
   if (is_split(d.precision)) {
     const bool bf16 = d.precision == LGB_SPLIT_BF16;
     cudaEvent_t ev[2];
-    if ((st = launch_maxabs_amp(amp, B, d.H, d.W, d.r0, d.c0, d.m, d.n, P->maxabs, s))) return st;
+    if ((st = launch_maxabs_amp(amp, B, d.H, d.W, d.r0, d.c0, d.m, d.n, ops.maxabs, s))) return st;
     SplitFieldArgs fa{};
     fa.amp = amp; fa.opd = opd;
     fa.H = d.H; fa.W = d.W; fa.r0 = d.r0; fa.c0 = d.c0;
     fa.khalf = P->khalf;
     fa.m = d.m; fa.n = d.n; fa.kp = P->kp1; fa.L = L; fa.batch = B;
-    fa.maxabs = P->maxabs;
-    fa.hi = P->fh; fa.lo = P->fl;
+    fa.maxabs = ops.maxabs;
+    fa.hi = ops.fh; fa.lo = ops.fl;
+    fa.lam_idx = lam_idx;
     if ((st = prof_begin(P, LGB_PROFILE_PHASOR, s, ev))) return st;
     if ((st = launch_split_field_T(fa, bf16, s))) return st;
     if ((st = prof_end(P, LGB_PROFILE_PHASOR, s, ev))) return st;
     SplitMftProblem p{};
     p.m = d.m; p.n = d.n; p.M = d.M; p.N = d.N; p.kp1 = P->kp1; p.kp2 = P->kp2;
     p.L = L; p.batch = B; p.bf16 = bf16;
-    p.e1_hi = P->e1h; p.e1_lo = P->e1l; p.f_hi = P->fh; p.f_lo = P->fl;
-    p.e2_hi = P->e2h; p.e2_lo = P->e2l; p.g_hi = P->gh; p.g_lo = P->gl;
-    p.maxabs = P->maxabs;
+    p.lam_idx = lam_idx;
+    p.L_bank = d.n_wavelengths;
+    p.e1_hi = P->e1h; p.e1_lo = P->e1l; p.f_hi = ops.fh; p.f_lo = ops.fl;
+    p.e2_hi = P->e2h; p.e2_lo = P->e2l; p.g_hi = ops.gh; p.g_lo = ops.gl;
+    p.maxabs = ops.maxabs;
     p.epilogue = 0;
     p.weights = weights;
     p.unit2 = P->unit2;
-    p.wbuf = P->wbuf;
-    p.ldw = P->ldw;
-    p.err = P->err;
-    LGB_CUDA(cudaMemsetAsync(P->wbuf, 0, sizeof(float) * (size_t)B * d.M * P->ldw, s));
+    p.wbuf = ops.wbuf;
+    p.ldw = ops.ldw;
+    p.err = errp;
+    LGB_CUDA(cudaMemsetAsync(ops.wbuf, 0, sizeof(float) * (size_t)B * d.M * ops.ldw, s));
     cudaEvent_t mev[4];
     if (P->profile) {
       for (auto& e : mev) LGB_CUDA(cudaEventCreate(&e));
@@ -416,7 +457,7 @@ static int psf_execute_n(lgb_psf_plan P, int B, const double* amp, const double*
       P->pending.push_back({LGB_PROFILE_MFT2, {mev[2], mev[3]}});
     }
     if ((st = prof_begin(P, LGB_PROFILE_OTHER, s, ev))) return st;
-    if ((st = launch_window_add(P->wbuf, d.M, d.N, P->ldw, B, out, d.out_cols, (long long)img,
+    if ((st = launch_window_add(ops.wbuf, d.M, d.N, ops.ldw, B, out, d.out_cols, (long long)img,
                                 d.win_r0, d.win_c0, s)))
       return st;
     return prof_end(P, LGB_PROFILE_OTHER, s, ev);
@@ -453,13 +494,43 @@ static int psf_execute_n(lgb_psf_plan P, int B, const double* amp, const double*
 extern "C" int lgb_psf_execute(lgb_psf_plan P, const double* amp, const double* opd,
                                const double* weights, double* out, int accumulate, lgb_stream stream) {
   LGB_REQUIRE(P, LGB_EINVAL, "psf_execute: null plan");
-  return psf_execute_n(P, P->d.batch, amp, opd, weights, out, accumulate, stream);
+  return psf_execute_n(P, P->d.batch, nullptr, 0, amp, opd, weights, out, accumulate, stream);
 }
 
 extern "C" int lgb_psf_execute_batch(lgb_psf_plan P, int count, const double* amp,
                                      const double* opd, const double* weights, double* out,
                                      int accumulate, lgb_stream stream) {
-  return psf_execute_n(P, count, amp, opd, weights, out, accumulate, stream);
+  return psf_execute_n(P, count, nullptr, 0, amp, opd, weights, out, accumulate, stream);
+}
+
+extern "C" size_t lgb_psf_execute_workspace_size(lgb_psf_plan P, int count, int n_sel) {
+  if (!P || count <= 0 || n_sel <= 0 || !is_split(P->d.precision)) return 0;
+  return carve_operands(nullptr, P->d, P->kp1, P->kp2, count, n_sel, nullptr);
+}
+
+extern "C" int lgb_psf_execute_ws(lgb_psf_plan P, int count, const int* lam_idx, int n_sel,
+                                  const double* amp, const double* opd, const double* weights,
+                                  double* out, int accumulate, void* workspace,
+                                  size_t workspace_bytes, lgb_stream stream) {
+  LGB_REQUIRE(P, LGB_EINVAL, "psf_execute_ws: null plan");
+  LGB_REQUIRE(is_split(P->d.precision), LGB_EUNSUPPORTED,
+              "psf_execute_ws: caller workspaces serve split-precision plans");
+  const int L = lam_idx ? n_sel : P->d.n_wavelengths;
+  LGB_REQUIRE(workspace && ((uintptr_t)workspace & 255) == 0, LGB_EWORKSPACE,
+              "psf_execute_ws: workspace must be non-null and 256-byte aligned");
+  LGB_REQUIRE(workspace_bytes >= lgb_psf_execute_workspace_size(P, count, L), LGB_EWORKSPACE,
+              "psf_execute_ws: workspace too small");
+  SplitOperands ops;
+  carve_operands(workspace, P->d, P->kp1, P->kp2, count, L, &ops);
+  return psf_execute_n(P, count, lam_idx, lam_idx ? n_sel : 0, amp, opd, weights, out,
+                       accumulate, stream, &ops);
+}
+
+extern "C" int lgb_psf_execute_subset(lgb_psf_plan P, int count, const int* lam_idx, int n_sel,
+                                      const double* amp, const double* opd, const double* weights,
+                                      double* out, int accumulate, lgb_stream stream) {
+  LGB_REQUIRE(lam_idx, LGB_EINVAL, "psf_execute_subset: null wavelength index");
+  return psf_execute_n(P, count, lam_idx, n_sel, amp, opd, weights, out, accumulate, stream);
 }
 
 extern "C" int lgb_psf_plan_profile(lgb_psf_plan P, int enable) {

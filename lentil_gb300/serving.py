@@ -3,17 +3,22 @@
 Requests (one broadband PSF each: pupil amplitude and OPD, wavelengths and
 weights, optics) are queued by any thread and scheduled by one GPU thread:
 
-- plans (the resident DFT matrices and operand buffers of one optics /
-  wavelength set) live in an LRU cache whose device bytes are admitted
-  against an HBM budget; idle plans are evicted to make room, a request that
-  alone exceeds the budget fails with MemoryError;
-- every scheduling pass takes the oldest request whose plan is idle,
-  batches the queued requests with the same plan (up to the plan's batch
-  capacity) and launches them on a free CUDA stream, so requests that arrive
-  while others run are admitted as plans and streams free up, and different
-  plans' work overlaps on the device;
-- each (plan, batch count) launch sequence is captured once into a CUDA
-  graph and replayed;
+- the server holds a spectral grid; a plan built on the grid (the resident
+  DFT matrices of every grid wavelength for one optics geometry) serves every
+  request whose wavelengths lie on the grid, by wavelength subset -- a
+  device-resident DFT-matrix cache.  Requests off the grid get a plan of
+  their own wavelengths;
+- plans live in an LRU cache whose device bytes are admitted against an HBM
+  budget; plans without launches in flight are evicted to make room, a
+  request whose plan alone exceeds the budget fails with MemoryError;
+- every scheduling pass takes the oldest request, batches the queued
+  requests with the same plan and wavelength subset (up to ``max_batch``)
+  and launches them on a free CUDA stream with operand buffers of their own,
+  so requests that arrive while others run are admitted as streams free up,
+  and launches (of the same plan or of different plans) overlap on the
+  device;
+- a small launch shape seen twice keeps its buffers and is captured into a
+  CUDA graph that later launches replay;
 - completion is detected with CUDA events; latency is submit -> result.
 """
 import collections
@@ -40,6 +45,8 @@ class PSFRequest:
         self.opd = np.ascontiguousarray(opd, dtype=np.float64)
         self.wavelengths = np.atleast_1d(np.asarray(wavelengths, dtype=np.float64))
         self.weights = np.atleast_1d(np.asarray(weights, dtype=np.float64))
+        if self.weights.shape != self.wavelengths.shape:
+            raise ValueError('one weight per wavelength')
         self.pixelscale_in = float(pixelscale_in)
         self.focal_length = float(focal_length)
         self.det_pixelscale = float(det_pixelscale)
@@ -47,17 +54,15 @@ class PSFRequest:
         self.oversample = int(oversample)
         self.future = concurrent.futures.Future()
         self.t_submit = self.t_done = None
+        self._geo_key = None
 
-    def key(self, precision):
-        k = getattr(self, '_key', None)
-        if k is None or k[0] != precision:
+    def geometry_key(self):
+        if self._geo_key is None:
             s = util.boundary_slice(self.amp)
-            k = (precision, (self.amp.shape, self.wavelengths.tobytes(), self.pixelscale_in,
-                             self.focal_length, self.det_pixelscale, self.det_shape,
-                             self.oversample, precision,
-                             (s[0].start, s[0].stop, s[1].start, s[1].stop)))
-            self._key = k
-        return k[1]
+            self._geo_key = (self.amp.shape, self.pixelscale_in, self.focal_length,
+                             self.det_pixelscale, self.det_shape, self.oversample,
+                             (s[0].start, s[0].stop, s[1].start, s[1].stop))
+        return self._geo_key
 
     @property
     def latency(self):
@@ -77,62 +82,109 @@ def plan_bytes_estimate(plane_shape, fslice, window, L, batch, precision):
     return e + ops
 
 
-class _Slot:
-    """A cached plan with static device/pinned buffers and captured graphs."""
+class _Buffers:
+    """Device and pinned host buffers of one launch shape (n PSFs, n_sel
+    wavelengths), optionally with the launch captured as a CUDA graph."""
 
-    def __init__(self, key, geo, batch, precision, device):
-        self.key, self.geo, self.batch = key, geo, batch
-        self.plan = make_plan(geo, batch=batch, precision=precision)
-        H, W = geo.plane_shape
-        L = len(geo.wavelengths)
-        self.A = torch.zeros((batch, H, W), dtype=torch.float64, device=device)
-        self.O = torch.zeros_like(self.A)
-        self.Wt = torch.zeros((batch, L), dtype=torch.float64, device=device)
-        self.out = torch.zeros((batch,) + geo.shape_out, dtype=torch.float64, device=device)
-        self.hA = torch.zeros((batch, H, W), dtype=torch.float64).pin_memory()
-        self.hO = torch.zeros_like(self.hA).pin_memory()
-        self.hW = torch.zeros((batch, L), dtype=torch.float64).pin_memory()
-        self.hout = torch.zeros((batch,) + geo.shape_out, dtype=torch.float64).pin_memory()
-        self.bytes = (self.plan.nbytes + 8 * (self.A.numel() * 2 + self.Wt.numel() + self.out.numel()))
-        self.graphs = {}
+    def __init__(self, slot, n, n_sel, device):
+        H, W = slot.geo.plane_shape
+        self.n, self.n_sel = n, n_sel
+        self.A = torch.empty((n, H, W), dtype=torch.float64, device=device)
+        self.O = torch.empty_like(self.A)
+        self.Wt = torch.empty(n * n_sel, dtype=torch.float64, device=device)
+        self.lam = torch.empty(n_sel, dtype=torch.int32, device=device)
+        self.out = torch.empty((n,) + slot.geo.shape_out, dtype=torch.float64, device=device)
+        self.ws = torch.empty(max(1, slot.plan.workspace_bytes(n, n_sel)), dtype=torch.uint8,
+                              device=device)
+        self.hA = torch.empty((n, H, W), dtype=torch.float64, pin_memory=True)
+        self.hO = torch.empty_like(self.hA, pin_memory=True)
+        self.hW = torch.empty(n * n_sel, dtype=torch.float64, pin_memory=True)
+        self.hlam = torch.empty(n_sel, dtype=torch.int32, pin_memory=True)
+        self.hout = torch.empty((n,) + slot.geo.shape_out, dtype=torch.float64, pin_memory=True)
+        self.graph = None
         self.busy = False
 
-    def run(self, n, stream, use_graphs):
-        """Launch the first n PSFs on ``stream`` (inputs already staged)."""
+    @property
+    def nbytes(self):
+        return 8 * (2 * self.A.numel() + self.Wt.numel() + self.out.numel()) + self.ws.numel()
+
+    def launch(self, slot):
+        lam = self.lam if slot.grid else None
+        slot.plan.execute(self.A, self.O, self.Wt, out=self.out, check=False, lam_idx=lam,
+                          workspace=self.ws)
+
+
+class _Slot:
+    """A cached plan: the resident DFT matrices of one optics geometry (and
+    wavelength grid); launches bring their own operand buffers."""
+
+    STATIC_LIMIT = 256 << 20      # launch shapes up to this size keep buffers + a graph
+
+    def __init__(self, key, geo, precision, grid):
+        self.key, self.geo, self.grid = key, geo, grid
+        self.plan = make_plan(geo, batch=0, precision=precision)
+        self.bytes = self.plan.nbytes
+        self.static = {}              # (n, n_sel) -> _Buffers reused across launches
+        self.seen = collections.Counter()
+        self.inflight = 0
+
+    def buffers(self, n, n_sel, device, use_graphs):
+        key = (n, n_sel)
+        self.seen[key] += 1
+        b = self.static.get(key)
+        if b is not None and not b.busy:
+            return b, True
+        b = _Buffers(self, n, n_sel, device)
+        if use_graphs and key not in self.static and self.seen[key] >= 2 and \
+                b.nbytes <= self.STATIC_LIMIT:
+            self.static[key] = b
+            return b, True
+        return b, False
+
+    def run(self, b, stream, reuse):
+        """Launch buffers ``b`` (host inputs already staged) on ``stream``."""
+        n, n_sel = b.n, b.n_sel
         with torch.cuda.stream(stream):
-            self.A[:n].copy_(self.hA[:n], non_blocking=True)
-            self.O[:n].copy_(self.hO[:n], non_blocking=True)
-            self.Wt[:n].copy_(self.hW[:n], non_blocking=True)
-            if use_graphs:
-                g = self.graphs.get(n)
-                if g is None:
-                    # warm up once outside capture, then capture the launch sequence
-                    self.plan.execute(self.A[:n], self.O[:n], self.Wt[:n], out=self.out[:n], check=False)
-                    g = torch.cuda.CUDAGraph()
-                    with torch.cuda.graph(g, stream=stream):
-                        self.plan.execute(self.A[:n], self.O[:n], self.Wt[:n], out=self.out[:n],
-                                          check=False)
-                    self.graphs[n] = g
-                g.replay()
+            b.A.copy_(b.hA, non_blocking=True)
+            b.O.copy_(b.hO, non_blocking=True)
+            b.Wt.copy_(b.hW, non_blocking=True)
+            if self.grid:
+                b.lam.copy_(b.hlam, non_blocking=True)
+            if reuse and b.graph is None:
+                b.launch(self)                       # warm-up outside capture
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=stream):
+                    b.launch(self)
+                b.graph = g
+            if b.graph is not None:
+                b.graph.replay()
             else:
-                self.plan.execute(self.A[:n], self.O[:n], self.Wt[:n], out=self.out[:n], check=False)
-            self.hout[:n].copy_(self.out[:n], non_blocking=True)
+                b.launch(self)
+            b.hout.copy_(b.out, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(stream)
         return ev
 
 
 class PSFServer:
-    """Continuous-batching broadband PSF server on one GPU."""
+    """Continuous-batching broadband PSF server on one GPU.
+
+    ``grid``: the spectral grid (metres) whose wavelengths share resident DFT
+    matrices; default 128 points over 400-1000 nm."""
 
     def __init__(self, hbm_budget=None, streams=4, max_batch=4, precision='split',
-                 use_graphs=True, device=None):
+                 use_graphs=True, grid=None, device=None):
         self.device = device or dv.device()
         free, total = torch.cuda.mem_get_info(self.device)
-        self.budget = int(hbm_budget) if hbm_budget else int(0.7 * free)
+        # budget for resident plans; launch buffers come on top, from the
+        # caching allocator, at most one launch per stream
+        self.budget = int(hbm_budget) if hbm_budget else int(0.55 * free)
         self.precision = precision
         self.max_batch = max_batch
         self.use_graphs = use_graphs
+        self.grid = np.asarray(np.linspace(400e-9, 1000e-9, 128) if grid is None else grid, float)
+        if precision == 'fp64':
+            self.grid = np.zeros(0)                   # wavelength subsets need split plans
         self.n_streams = streams
         self._queue = collections.deque()
         self._cv = threading.Condition()
@@ -143,7 +195,6 @@ class PSFServer:
         self._streams = []
         self._stop = False
         self.stats = collections.Counter()
-        self._error = None
         self._thread = threading.Thread(target=self._loop, name='psf-server', daemon=True)
         self._thread.start()
 
@@ -152,6 +203,7 @@ class PSFServer:
         if req.future.done():                      # a request object may be submitted again
             req.future = concurrent.futures.Future()
             req.t_done = None
+        self._classify(req)
         req.t_submit = time.perf_counter()
         with self._cv:
             if self._stop:
@@ -184,6 +236,26 @@ class PSFServer:
     def __exit__(self, *exc):
         self.close()
 
+    # ---------------------------------------------------------- requests
+    def _classify(self, req):
+        """Plan key, wavelength subset on the grid (or None) and batch key."""
+        idx = None
+        if len(self.grid):
+            pos = np.clip(np.searchsorted(self.grid, req.wavelengths), 0, len(self.grid) - 1)
+            lo = np.clip(pos - 1, 0, len(self.grid) - 1)
+            pick = np.where(np.abs(self.grid[lo] - req.wavelengths) <
+                            np.abs(self.grid[pos] - req.wavelengths), lo, pos)
+            on = np.abs(self.grid[pick] - req.wavelengths) <= 1e-9 * req.wavelengths
+            if np.all(on) and len(np.unique(pick)) == len(pick):
+                idx = pick.astype(np.int32)
+        req._subset = idx
+        if idx is not None:
+            req._plan_key = ('grid', req.geometry_key(), self.precision)
+            req._batch_key = (req._plan_key, idx.tobytes())
+        else:
+            req._plan_key = ('own', req.geometry_key(), req.wavelengths.tobytes(), self.precision)
+            req._batch_key = (req._plan_key, b'')
+
     # ---------------------------------------------------------- scheduler
     def _loop(self):
         torch.cuda.set_device(self.device)
@@ -200,11 +272,11 @@ class PSFServer:
     def _poll(self):
         done = [x for x in self._inflight if x[0].query()]
         for item in done:
-            ev, slot, reqs, si = item
+            ev, slot, b, reqs, si = item
             self._inflight.remove(item)
             now = time.perf_counter()
             try:
-                _lib.call('lgb_psf_plan_status', slot.plan._h, self._streams[si].cuda_stream)
+                _lib.call('lgb_dft2_status', b.ws.data_ptr(), self._streams[si].cuda_stream)
                 err = None
             except Exception as e:                     # device timeout or CUDA error
                 err = e
@@ -213,26 +285,21 @@ class PSFServer:
                 if r.future.done():
                     continue
                 if err is None:
-                    r.future.set_result(slot.hout[k].numpy().copy())
+                    r.future.set_result(b.hout[k].numpy().copy())
                 else:
                     r.future.set_exception(err)
-            slot.busy = False
+            b.busy = False
+            slot.inflight -= 1
             self._free_streams.append(si)
             self.stats['completed'] += len(reqs)
         return bool(done)
-
-    def _geometry(self, req):
-        s = util.boundary_slice(req.amp)
-        return plan_geometry(req.amp.shape, s, [], np.broadcast_to(req.pixelscale_in, (2,)),
-                             req.focal_length, PUPIL, req.wavelengths, req.det_pixelscale,
-                             shape=req.det_shape, oversample=req.oversample)
 
     def _make_room(self, need):
         for key in list(self._slots):
             if self._bytes + need <= self.budget:
                 break
             slot = self._slots[key]
-            if not slot.busy:
+            if slot.inflight == 0:
                 del self._slots[key]
                 self._bytes -= slot.bytes
                 del slot
@@ -240,32 +307,32 @@ class PSFServer:
         return self._bytes + need <= self.budget
 
     def _slot_for(self, req):
-        key = req.key(self.precision)
+        key = req._plan_key
         slot = self._slots.get(key)
         if slot is not None:
             self._slots.move_to_end(key)
             self.stats['plan_hits'] += 1
-            return slot, key
-        geo = self._geometry(req)
-        if geo.window_shape is None:
-            return 'empty', key
+            return slot
+        grid = req._subset is not None
+        wl = self.grid if grid else req.wavelengths
+        s = util.boundary_slice(req.amp)
+        geo = plan_geometry(req.amp.shape, s, [], np.broadcast_to(req.pixelscale_in, (2,)),
+                            req.focal_length, PUPIL, wl, req.det_pixelscale,
+                            shape=req.det_shape, oversample=req.oversample)
+        if geo.window_shape is None or (grid and len(geo.keep) != len(wl)):
+            return 'empty'
         L = len(geo.wavelengths)
-        batch = self.max_batch
-        est = plan_bytes_estimate(geo.plane_shape, geo.fslice, geo.window_shape, L, batch,
+        est = plan_bytes_estimate(geo.plane_shape, geo.fslice, geo.window_shape, L, 0,
                                   self.precision)
-        while batch > 1 and est > self.budget // 4:
-            batch //= 2
-            est = plan_bytes_estimate(geo.plane_shape, geo.fslice, geo.window_shape, L, batch,
-                                      self.precision)
         if est > self.budget:
-            return 'too_big', key
-        if not self._make_room(int(est * 1.1)):
-            return None, key                          # wait for running work to finish
-        slot = _Slot(key, geo, batch, self.precision, self.device)
+            return 'too_big'
+        if not self._make_room(int(est * 1.05)):
+            return None                               # wait for running work to finish
+        slot = _Slot(key, geo, self.precision, grid)
         self._slots[key] = slot
         self._bytes += slot.bytes
         self.stats['plans_built'] += 1
-        return slot, key
+        return slot
 
     def _admit(self):
         progressed = False
@@ -275,48 +342,48 @@ class PSFServer:
             if not pending:
                 break
             chosen = None
-            for req in pending:                       # oldest request whose plan is free
-                key = req.key(self.precision)
-                s = self._slots.get(key)
-                if s is not None and s.busy:
-                    continue
-                slot, key = self._slot_for(req)
-                if slot == 'too_big':
+            for req in pending:                       # oldest request first
+                slot = self._slot_for(req)
+                if isinstance(slot, str):             # 'too_big' or 'empty'
                     with self._cv:
                         self._queue.remove(req)
-                    req.future.set_exception(MemoryError(
-                        'request needs more device memory than the server budget'))
-                    self.stats['rejected'] += 1
-                    progressed = True
-                    continue
-                if slot == 'empty':
-                    with self._cv:
-                        self._queue.remove(req)
-                    req.t_done = time.perf_counter()
-                    req.future.set_result(np.zeros((req.det_shape * req.oversample,) * 2))
+                    if slot == 'too_big':
+                        req.future.set_exception(MemoryError(
+                            'request needs more device memory than the server budget'))
+                        self.stats['rejected'] += 1
+                    else:
+                        req.t_done = time.perf_counter()
+                        req.future.set_result(np.zeros((req.det_shape * req.oversample,) * 2))
                     progressed = True
                     continue
                 if slot is None:
                     continue
-                chosen = (slot, key)
+                chosen = (slot, req._batch_key)
                 break
             if chosen is None:
                 break
-            slot, key = chosen
+            slot, bkey = chosen
             with self._cv:
-                batch = [r for r in self._queue if r.key(self.precision) == key][:slot.batch]
+                batch = [r for r in self._queue if r._batch_key == bkey][:self.max_batch]
                 for r in batch:
                     self._queue.remove(r)
-            keep = slot.geo.keep
+            n_sel = len(batch[0].wavelengths) if slot.grid else len(slot.geo.wavelengths)
+            b, reuse = slot.buffers(len(batch), n_sel, self.device, self.use_graphs)
+            hW = b.hW.view(len(batch), n_sel).numpy()
             for k, r in enumerate(batch):
-                slot.hA[k].numpy()[...] = r.amp
-                slot.hO[k].numpy()[...] = r.opd
-                slot.hW[k].numpy()[...] = r.weights[keep]
+                b.hA[k].numpy()[...] = r.amp
+                b.hO[k].numpy()[...] = r.opd
+                hW[k] = r.weights if slot.grid else r.weights[slot.geo.keep]
+            if slot.grid:
+                b.hlam.numpy()[...] = batch[0]._subset
             si = self._free_streams.pop(0)
-            slot.busy = True
-            ev = slot.run(len(batch), self._streams[si], self.use_graphs)
-            self._inflight.append((ev, slot, batch, si))
+            b.busy = True
+            slot.inflight += 1
+            ev = slot.run(b, self._streams[si], reuse)
+            self._inflight.append((ev, slot, b, batch, si))
             self.stats['launches'] += 1
             self.stats['batched'] += len(batch)
+            if b.graph is not None:
+                self.stats['graph_launches'] += 1
             progressed = True
         return progressed

@@ -77,9 +77,29 @@ def test_budget_rejects_oversize_and_cancel(cuda_device):
 def test_eviction_under_budget(cuda_device):
     rng = np.random.default_rng(9)
     reqs = [_request(rng, 64, 16, L) for L in (2, 3, 4, 5, 6)]
-    one = serving.plan_bytes_estimate((64, 64), (0, 0, 58, 58), (32, 32), 6, 1, 'split')
-    with serving.PSFServer(hbm_budget=int(2.5 * one), streams=1, max_batch=1) as srv:
+    one = serving.plan_bytes_estimate((64, 64), (0, 0, 58, 58), (32, 32), 6, 0, 'split')
+    with serving.PSFServer(hbm_budget=int(2.5 * one), streams=1, max_batch=1,
+                           grid=np.zeros(0)) as srv:
         out = [srv.submit(r).result(timeout=120) for r in reqs]
         assert srv.stats['evicted'] >= 1
+    for r, img in zip(reqs, out):
+        assert lo.peak_normalised_error(img, _alone(r)) < TOL
+
+
+def test_grid_plans_serve_wavelength_subsets(cuda_device):
+    # requests whose wavelengths lie on the server grid share one resident
+    # plan per optics geometry (DFT-matrix cache) whatever their subset
+    rng = np.random.default_rng(10)
+    grid = np.linspace(400e-9, 1000e-9, 16)
+    reqs = []
+    for L in (1, 3, 5, 16, 2, 7):
+        r = _request(rng, 64, 16, L)
+        idx = np.sort(rng.choice(16, L, replace=False))
+        r.wavelengths, r.weights = grid[idx], rng.uniform(0.5, 1.5, L)
+        reqs.append(r)
+    with serving.PSFServer(streams=2, max_batch=2, grid=grid) as srv:
+        out = [f.result(timeout=120) for f in [srv.submit(r) for r in reqs]]
+        stats = dict(srv.stats)
+    assert stats['plans_built'] == 1
     for r, img in zip(reqs, out):
         assert lo.peak_normalised_error(img, _alone(r)) < TOL
