@@ -1,13 +1,16 @@
 // K6: detector pixel MTF and pixelation (lentil/detector.py:167-251).
 //
 // lentil applies the pixel MTF as |ifft2(fft2(img) * (s (x) s))| with
-// s[k] = sinc(fftfreq(N)[k] * os) (lentil/detector.py:218-222).  For a square
-// N x N image that is |C . img . C^T| with C the real symmetric circulant
-// C[i][j] = c[(i - j) mod N], c = ifft(s): two real GEMMs on the FP64 pipe,
-// the form used here.  pixelate then resamples by 1/os with a cubic spline
-// (lentil/util.py:261-349); when N is a multiple of os every sample falls on
-// a grid point, so the result is d = p[::os, ::os] rescaled by
-// sum(p)/sum(d) and masked where d == 0 -- the only case implemented.
+// s[k] = sinc(fftfreq(N)[k] * os) (lentil/detector.py:218-222), for square
+// N x N images.  Two FP64 evaluations of that product:
+//   - N a power of two (<= 8192): the same FFT form, with this file's
+//     shared-memory radix-2 row FFTs and tiled transposes (~10 N^2 log2 N flop);
+//   - any other N: |C . img . C^T| with C the real symmetric circulant
+//     C[i][j] = c[(i - j) mod N], c = ifft(s), as two FP64 GEMMs.
+// pixelate then resamples by 1/os with a cubic spline (lentil/util.py:261-349);
+// when N is a multiple of os every sample falls on a grid point, so the
+// result is d = p[::os, ::os] rescaled by sum(p)/sum(d) and masked where
+// d == 0 -- the only case implemented.
 #include <algorithm>
 #include <cmath>
 
@@ -16,17 +19,89 @@
 
 namespace lgb {
 
-// c[k] = (1/N) sum_f s_f cos(2 pi f k / N), s_f = sinc(freq_f * os)
+__device__ __forceinline__ double sinc_os(int k, int N, double os) {
+  const int ff = (k < (N + 1) / 2) ? k : k - N;          // numpy fftfreq ordering
+  const double x = (double)ff / N * os;
+  return (x == 0.0) ? 1.0 : sinpi(x) / (M_PI * x);
+}
+
+// ---------------------------------------------------------------- FFT path
+__global__ void twiddle_kernel(int N, double2* __restrict__ tw) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N / 2) return;
+  double s, c;
+  sincospi(-2.0 * (double)k / N, &s, &c);                 // exp(-2 pi i k / N)
+  tw[k] = make_double2(c, s);
+}
+
+__global__ void real_to_complex_kernel(const double* __restrict__ x, double2* __restrict__ z,
+                                       size_t count) {
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < count;
+       p += (size_t)gridDim.x * blockDim.x)
+    z[p] = make_double2(x[p], 0.0);
+}
+
+// In-place FFT of every row (length N = 2^logN) in shared memory.
+__global__ void __launch_bounds__(512) fft_rows_kernel(double2* __restrict__ data, int N, int logN,
+                                                       const double2* __restrict__ tw,
+                                                       int inverse) {
+  extern __shared__ double2 sm[];
+  double2* row = data + (size_t)blockIdx.x * N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x)
+    sm[__brev((unsigned)i) >> (32 - logN)] = row[i];
+  __syncthreads();
+  for (int s = 1; s <= logN; ++s) {
+    const int half = 1 << (s - 1);
+    const int stride = N >> s;                         // twiddle index step
+    for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+      const int pos = b & (half - 1);
+      const int i0 = ((b >> (s - 1)) << s) + pos, i1 = i0 + half;
+      double2 w = tw[pos * stride];
+      if (inverse) w.y = -w.y;
+      const double2 a = sm[i0], v = sm[i1];
+      const double2 t = make_double2(w.x * v.x - w.y * v.y, w.x * v.y + w.y * v.x);
+      sm[i0] = make_double2(a.x + t.x, a.y + t.y);
+      sm[i1] = make_double2(a.x - t.x, a.y - t.y);
+    }
+    __syncthreads();
+  }
+  const double scale = inverse ? 1.0 / N : 1.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x)
+    row[i] = make_double2(sm[i].x * scale, sm[i].y * scale);
+}
+
+// out = in^T (N x N complex128), 32 x 32 tiles
+__global__ void transpose_c128_kernel(const double2* __restrict__ in, double2* __restrict__ out,
+                                      int N) {
+  __shared__ double2 t[32][33];
+  const int x = blockIdx.x * 32 + threadIdx.x, y0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y)
+    if (x < N && y0 + k < N) t[k][threadIdx.x] = in[(size_t)(y0 + k) * N + x];
+  __syncthreads();
+  const int xo = blockIdx.y * 32 + threadIdx.x, yo0 = blockIdx.x * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y)
+    if (xo < N && yo0 + k < N) out[(size_t)(yo0 + k) * N + xo] = t[threadIdx.x][k];
+}
+
+// z[i][j] *= s[i] s[j]  (the separable pixel MTF; symmetric in i, j)
+__global__ void mtf_multiply_kernel(double2* __restrict__ z, int N, double os) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= N) return;
+  const double k = sinc_os(i, N, os) * sinc_os(j, N, os);
+  double2 v = z[(size_t)i * N + j];
+  z[(size_t)i * N + j] = make_double2(v.x * k, v.y * k);
+}
+
+// ------------------------------------------------------------- GEMM path
+// c[k] = (1/N) sum_f s_f cos(2 pi f k / N)
 __global__ void pixel_taps_kernel(int N, double os, double* __restrict__ c) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= N) return;
   double acc = 0.0;
   for (int f = 0; f < N; ++f) {
-    const int ff = (f < (N + 1) / 2) ? f : f - N;        // numpy fftfreq ordering
-    const double x = (double)ff / N * os;
-    const double s = (x == 0.0) ? 1.0 : sinpi(x) / (M_PI * x);
     const long long ph = ((long long)f * k) % N;         // exact phase index
-    acc += s * cospi(2.0 * (double)ph / N);
+    acc += sinc_os(f, N, os) * cospi(2.0 * (double)ph / N);
   }
   c[k] = acc / N;
 }
@@ -86,23 +161,33 @@ __global__ void __launch_bounds__(256) dgemm_kernel(int N, const double* __restr
     }
 }
 
+// ---------------------------------------------------------- common tail
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-// p = |P| in place; sums[0] += sum |P|, and the decimated samples
-// d[k][l] = |P[k*os][l*os]| with sums[1] += sum d
-__global__ void pixel_abs_reduce_kernel(int N, int os, double* __restrict__ P,
-                                        double* __restrict__ d, double* __restrict__ sums) {
+// p = |value| written to P; sums[0] += sum p; decimated samples
+// d[k][l] = p[k*os][l*os] with sums[1] += sum d.  Reads a real (GEMM path)
+// or complex (FFT path) array.
+template <bool COMPLEX>
+__global__ void pixel_abs_reduce_kernel(int N, int os, const void* __restrict__ src,
+                                        double* __restrict__ P, double* __restrict__ d,
+                                        double* __restrict__ sums) {
   double s_all = 0.0, s_dec = 0.0;
   const size_t total = (size_t)N * N;
   const int Nd = N / os;
   for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < total;
        p += (size_t)gridDim.x * blockDim.x) {
-    const double v = fabs(P[p]);
-    P[p] = v;
+    double v;
+    if (COMPLEX) {
+      const double2 z = static_cast<const double2*>(src)[p];
+      v = hypot(z.x, z.y);
+    } else {
+      v = fabs(static_cast<const double*>(src)[p]);
+    }
+    if (P) P[p] = v;
     s_all += v;
     const int i = (int)(p / N), j = (int)(p % N);
     if (d && i % os == 0 && j % os == 0) {
@@ -127,40 +212,95 @@ __global__ void pixelate_scale_kernel(int count, const double* __restrict__ d,
   out[p] = (v != 0.0) ? v * (sums[0] / sums[1]) : 0.0;
 }
 
+static bool fft_size(int N, int* logN) {
+  if (N < 2 || N > 8192 || (N & (N - 1))) return false;
+  int l = 0;
+  while ((1 << l) < N) ++l;
+  *logN = l;
+  return true;
+}
+
 struct PixelSpace {
-  double *c, *C, *T, *P, *d, *sums;
+  double* sums;
+  double* d;
+  // GEMM path
+  double *c, *C, *T, *P;
+  // FFT path
+  double2 *X, *Y, *tw;
 };
 
 static size_t pixel_space(void* ws, int N, int os, PixelSpace* s) {
   size_t off = 0;
-  auto take = [&](size_t n) {
+  auto take = [&](size_t bytes) {
     off = align_up(off, 256);
-    double* p = ws ? reinterpret_cast<double*>(static_cast<char*>(ws) + off) : nullptr;
-    off += n * sizeof(double);
+    void* p = ws ? static_cast<char*>(ws) + off : nullptr;
+    off += bytes;
     return p;
   };
-  PixelSpace t;
-  t.sums = take(4);
-  t.c = take(N);
-  t.C = take((size_t)N * N);
-  t.T = take((size_t)N * N);
-  t.P = take((size_t)N * N);
-  t.d = take((size_t)(N / std::max(os, 1)) * (N / std::max(os, 1)));
+  PixelSpace t{};
+  int logN;
+  const size_t NN = (size_t)N * N;
+  const int Nd = N / std::max(os, 1);
+  t.sums = static_cast<double*>(take(4 * sizeof(double)));
+  t.d = static_cast<double*>(take((size_t)Nd * Nd * sizeof(double)));
+  if (fft_size(N, &logN)) {
+    t.X = static_cast<double2*>(take(NN * sizeof(double2)));
+    t.Y = static_cast<double2*>(take(NN * sizeof(double2)));
+    t.tw = static_cast<double2*>(take((size_t)(N / 2) * sizeof(double2)));
+  } else {
+    t.c = static_cast<double*>(take(N * sizeof(double)));
+    t.C = static_cast<double*>(take(NN * sizeof(double)));
+    t.T = static_cast<double*>(take(NN * sizeof(double)));
+    t.P = static_cast<double*>(take(NN * sizeof(double)));
+  }
   if (s) *s = t;
   return off;
 }
 
-static int run_pixel(const double* img, int N, int os, void* ws, cudaStream_t s, PixelSpace* w) {
+// Runs the MTF product; returns (src, complex?) of the pre-abs result.
+static int run_pixel(const double* img, int N, int os, void* ws, cudaStream_t s, PixelSpace* w,
+                     const void** src, bool* is_complex) {
   pixel_space(ws, N, os, w);
   LGB_CUDA(cudaMemsetAsync(w->sums, 0, 4 * sizeof(double), s));
+  int logN;
+  if (fft_size(N, &logN)) {
+    const size_t NN = (size_t)N * N;
+    const int blocks = std::max(1, std::min(4 * sm_count(), (int)((NN + 255) / 256)));
+    twiddle_kernel<<<cdiv(std::max(N / 2, 1), 256), 256, 0, s>>>(N, w->tw);
+    real_to_complex_kernel<<<blocks, 256, 0, s>>>(img, w->X, NN);
+    const size_t smem = (size_t)N * sizeof(double2);
+    LGB_CUDA(cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  8192 * (int)sizeof(double2)));
+    const int threads = std::min(512, std::max(32, N / 2));
+    const dim3 tgrid(cdiv(N, 32), cdiv(N, 32)), tblock(32, 8);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w->X, N, logN, w->tw, 0);       // rows
+    transpose_c128_kernel<<<tgrid, tblock, 0, s>>>(w->X, w->Y, N);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w->Y, N, logN, w->tw, 0);       // columns
+    mtf_multiply_kernel<<<dim3(cdiv(N, 128), N), 128, 0, s>>>(w->Y, N, (double)os);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w->Y, N, logN, w->tw, 1);
+    transpose_c128_kernel<<<tgrid, tblock, 0, s>>>(w->Y, w->X, N);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w->X, N, logN, w->tw, 1);
+    LGB_CUDA(cudaGetLastError());
+    *src = w->X;
+    *is_complex = true;
+    return LGB_OK;
+  }
   pixel_taps_kernel<<<cdiv(N, 128), 128, 0, s>>>(N, (double)os, w->c);
-  LGB_CUDA(cudaGetLastError());
   circulant_kernel<<<dim3(cdiv(N, 128), N), 128, 0, s>>>(N, w->c, w->C);
-  LGB_CUDA(cudaGetLastError());
   dim3 grid(cdiv(N, DBN), cdiv(N, DBM));
   dgemm_kernel<<<grid, 256, 0, s>>>(N, w->C, img, w->T);      // T = C . img
-  LGB_CUDA(cudaGetLastError());
   dgemm_kernel<<<grid, 256, 0, s>>>(N, w->T, w->C, w->P);     // P = T . C^T (C symmetric)
+  LGB_CUDA(cudaGetLastError());
+  *src = w->P;
+  *is_complex = false;
+  return LGB_OK;
+}
+
+static int abs_reduce(int N, int os, const void* src, bool cplx, double* P, double* d,
+                      double* sums, cudaStream_t s) {
+  const int blocks = std::max(1, std::min(4 * sm_count(), cdiv(N * N, 256)));
+  if (cplx) pixel_abs_reduce_kernel<true><<<blocks, 256, 0, s>>>(N, os, src, P, d, sums);
+  else pixel_abs_reduce_kernel<false><<<blocks, 256, 0, s>>>(N, os, src, P, d, sums);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }
@@ -184,13 +324,11 @@ extern "C" int lgb_pixel(const double* img, int rows, int cols, int oversample, 
   const int N = rows;
   cudaStream_t s = as_stream(stream);
   PixelSpace w;
-  int st = run_pixel(img, N, oversample, workspace, s, &w);
+  const void* src;
+  bool cplx;
+  int st = run_pixel(img, N, oversample, workspace, s, &w, &src, &cplx);
   if (st) return st;
-  const int blocks = std::max(1, std::min(4 * sm_count(), cdiv(N * N, 256)));
-  pixel_abs_reduce_kernel<<<blocks, 256, 0, s>>>(N, 1, w.P, nullptr, w.sums);
-  LGB_CUDA(cudaGetLastError());
-  LGB_CUDA(cudaMemcpyAsync(out, w.P, sizeof(double) * (size_t)N * N, cudaMemcpyDeviceToDevice, s));
-  return LGB_OK;
+  return abs_reduce(N, 1, src, cplx, out, nullptr, w.sums, s);
 }
 
 extern "C" int lgb_pixelate(const double* img, int rows, int cols, int oversample, double* out,
@@ -206,11 +344,11 @@ extern "C" int lgb_pixelate(const double* img, int rows, int cols, int oversampl
   const int N = rows, os = oversample, Nd = N / os;
   cudaStream_t s = as_stream(stream);
   PixelSpace w;
-  int st = run_pixel(img, N, os, workspace, s, &w);
+  const void* src;
+  bool cplx;
+  int st = run_pixel(img, N, os, workspace, s, &w, &src, &cplx);
   if (st) return st;
-  const int blocks = std::max(1, std::min(4 * sm_count(), cdiv(N * N, 256)));
-  pixel_abs_reduce_kernel<<<blocks, 256, 0, s>>>(N, os, w.P, w.d, w.sums);
-  LGB_CUDA(cudaGetLastError());
+  if ((st = abs_reduce(N, os, src, cplx, nullptr, w.d, w.sums, s))) return st;
   pixelate_scale_kernel<<<cdiv(Nd * Nd, 256), 256, 0, s>>>(Nd * Nd, w.d, w.sums, out);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;

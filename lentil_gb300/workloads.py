@@ -84,3 +84,42 @@ def monochromatic_circle(seed=1):
                         for j in range(2, 12)])
     return Workload('monochromatic_circle', amp, None, basis, np.full(10, 20e-9),
                     np.array([650e-9]), np.array([1.0]), 1.0 / npix, 10.0, 5e-6, 128, 2, seed)
+
+
+def large_segmented(npix=4096, n_wavelengths=32, seed=5, tilt_lambda_d=50.0):
+    """Large oversampled broadband workload: ``npix``^2 pupil of the 18-hex
+    segmented aperture (gaps 2 px per 1024) with a central obscuration of 20 %
+    of the diameter and 3 spider vanes 8 px wide at 90/210/330 degrees; OPD =
+    Noll 2-22 N(0, 15 nm) + a seeded 1/f^2 PSD surface of 25 nm rms + a
+    global tilt of ``tilt_lambda_d`` lambda/D (at 800 nm) that fit_tilt turns
+    into an output shift; 32 wavelengths over 600-1000 nm with 5800 K
+    blackbody weights; 1024^2 detector at oversample 4 (scaled with npix),
+    then pixelated.  Returns (Workload, 2-D mask, opd with the tilt)."""
+    scale = npix / 1024
+    segs = shapes.hex_segments(rings=2, seg_radius=116.8 * scale, seg_gap=2 * scale)
+    gmask = util.pad(np.sum(segs, axis=0), (npix, npix))
+    obsc = shapes.circle((npix, npix), 0.2 * npix / 2)
+    mask = np.clip(gmask - obsc, 0, 1)
+    for ang in (90, 210, 330):
+        mask = mask * shapes.spider((npix, npix), 8 * scale, angle=ang)
+    amp = util.normalize_power(mask)
+    rng = np.random.default_rng(seed)
+    support = mask > 0
+    rho, theta = zernike_coordinates(support)
+    opd = np.zeros((npix, npix))
+    for j, c in zip(range(2, 23), rng.normal(0, 15e-9, 21)):
+        opd += c * zernike_mode(support, j, rho=rho, theta=theta)
+    from .wfe import power_spectrum
+    opd += power_spectrum(support, 1.0 / npix, 25e-9, 10.0, 2, seed=seed)
+    # tilt of tilt_lambda_d lambda/D at 800 nm in a random direction: Noll
+    # Z2/Z3 = 2 rho cos/sin, so a coefficient c gives 4c of OPD across D
+    ang = rng.uniform(0, 2 * np.pi)
+    c = tilt_lambda_d * 800e-9 / 4
+    opd += c * np.cos(ang) * zernike_mode(support, 2, rho=rho, theta=theta)
+    opd += c * np.sin(ang) * zernike_mode(support, 3, rho=rho, theta=theta)
+    wl_nm = np.linspace(600.0, 1000.0, n_wavelengths)
+    w = blackbody_photlam(wl_nm, 5800.0)
+    wl = Workload('large_segmented', amp, None, np.zeros((0, npix, npix), np.float32),
+                  np.zeros(0), wl_nm * 1e-9, w / w.sum(), 1.0 / npix, 10.0, 5e-6,
+                  npix // 4, 4, seed)
+    return wl, mask, opd

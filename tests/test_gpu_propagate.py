@@ -211,3 +211,24 @@ def test_pixel_unitary_and_errors(cuda_device):
         lg.detector.pixel(np.ones((10, 12)), 2)
     with pytest.raises(NotImplementedError):
         lg.detector.pixelate(np.ones((10, 10)), 3)
+
+
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-11), ('split-bf16', 3e-6)])
+def test_large_oversampled_pixelated_small_scale(cuda_device, precision, tol):
+    # the large oversampled workload at reduced size: obscured 18-hex pupil
+    # with spiders, PSD error and a large tilt removed by fit_tilt (output
+    # shift), oversample 4, then pixelate
+    from lentil_gb300 import workloads
+    wl, mask, opd = workloads.large_segmented(npix=256, n_wavelengths=3, tilt_lambda_d=6.0)
+    lam, w = wl.wavelengths, wl.weights
+    kw = dict(shape=64, oversample=4)
+    po = lo.Pupil(amplitude=wl.amp, opd=opd.copy(), pixelscale=wl.pixelscale_in, focal_length=10)
+    po.fit_tilt(inplace=True)
+    ref = lo.pixelate(lo.broadband_psf(po, lam, w, wl.det_pixelscale, **kw), 4)
+    pg = lg.Pupil(amplitude=wl.amp, opd=opd.copy(), pixelscale=wl.pixelscale_in, focal_length=10)
+    pg.fit_tilt(inplace=True)
+    assert len(pg.tilt) == 1
+    img = lg.detector.pixelate(lg.broadband_psf(pg, lam, w, wl.det_pixelscale,
+                                                precision=precision, **kw), 4)
+    assert img.shape == ref.shape == (64, 64)
+    assert lo.peak_normalised_error(img, ref) < tol
