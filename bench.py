@@ -38,7 +38,7 @@ TRAFFIC_FILE = os.path.join(ROOT, 'profiles', 'mft_split_broadband_segmented.jso
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--steps', type=int, default=200)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--batch', type=int, default=1, help='PSFs per step')
@@ -125,39 +125,58 @@ def run_reference(args):
 # GPU arm
 # --------------------------------------------------------------------------
 class ClockSampler:
-    """nvidia-smi clocks/throttle sampling while the timed region runs."""
+    """nvidia-smi clocks/throttle sampling while the timed region runs.
+
+    The sampler is started first and the timed region begins only once it has
+    produced a sample (nvidia-smi takes ~1 s to start); samples are stamped on
+    arrival and only those inside the timed region are summarised."""
     Q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
          'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
          'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
 
     def __init__(self, index):
-        self.index, self.proc = index, None
+        self.index, self.proc, self.stamped = index, None, []
+        self.t_in = self.t_out = None
+
+    def _reader(self):
+        for ln in self.proc.stdout:
+            if ln.strip():
+                self.stamped.append((time.perf_counter(), ln))
 
     def __enter__(self):
+        import threading
         try:
             self.proc = subprocess.Popen(
                 ['nvidia-smi', '-i', str(self.index), f'--query-gpu={self.Q}',
-                 '--format=csv,noheader,nounits', '-lms', '20'],
+                 '--format=csv,noheader,nounits', '-lms', '50'],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+            return self
+        threading.Thread(target=self._reader, daemon=True).start()
+        t0 = time.perf_counter()
+        while not self.stamped and time.perf_counter() - t0 < 5.0:
+            time.sleep(0.02)
+        self.t_in = time.perf_counter()
         return self
 
     def __exit__(self, *exc):
-        self.lines = []
+        self.t_out = time.perf_counter()
         if self.proc is not None:
+            time.sleep(0.06)
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+                self.proc.wait()
 
     def summary(self):
         sm, smax, power, reasons = [], [], [], set()
         names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
-        for ln in getattr(self, 'lines', []):
+        lines = [ln for t, ln in self.stamped
+                 if self.t_in is not None and self.t_in <= t <= self.t_out]
+        for ln in lines:
             f = [x.strip() for x in ln.split(',')]
             if len(f) < 8:
                 continue
@@ -171,7 +190,8 @@ class ClockSampler:
         if not sm:
             return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': [], 'samples': 0}
         return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(smax),
-                'power_w_max': max(power), 'reasons': sorted(reasons), 'samples': len(sm)}
+                'power_w_max': max(power), 'reasons': sorted(reasons), 'samples': len(sm),
+                'window_s': self.t_out - self.t_in}
 
 
 def peaks():

@@ -15,20 +15,33 @@
 //
 // Accumulation.  The tensor core's FP32 accumulate rounds toward zero on
 // every MMA, a bias that grows with the length of the accumulation chain
-// (measured: 1.8e-5 relative at K = 2048).  So the dominant hi.hi products
-// are accumulated in short chains: TMEM region X is restarted every KSUB
-// (= 4, one 64-wide K block) k-steps and the epilogue warps fold each chunk into round-to-nearest FP32
-// registers, while the MMA issues the small cross terms into region Y (one
-// long chain; its truncation is 2^-8 smaller).  The epilogue drain of X
-// hides behind the Y instructions.
+// (measured: 1.8e-5 relative at K = 2048 with one chain per tile).  So every
+// 64-wide K block is its own short chain: its 12 MMAs (4 k-steps x 3 split
+// products) go into one of two TMEM accumulators, the small cross terms
+// hi.lo + lo.hi first and the dominant hi.hi last, so that only the last 4
+// MMAs round at full magnitude.  The epilogue warps fold each block into
+// round-to-nearest FP32 registers while the MMA fills the other accumulator.
 //
-// Warp roles (320 threads, one CTA per SM, persistent over work items):
-//   warp 0       TMA producer (one lane)
-//   warp 1       TMEM allocator + MMA issuer (one lane)
+// CTA pairs (cta_group::2).  Two CTAs of a cluster run on a TPC's two SMs
+// and compute one 256 x 256 output tile together: CTA r holds rows
+// 128r..128r+127 of the A tile and rows 128r..128r+127 of the B tile in its
+// own shared memory, and one tcgen05.mma (M=256, N=256, K=16) issued by the
+// even CTA reads both halves.  Each SM thus fetches 64 KB per 64-wide K block
+// instead of the 96 KB a lone M=128 x N=256 CTA needs for the same MMA work,
+// and three stages fit in shared memory.
+//
+// Warp roles (320 threads per CTA, one CTA per SM, persistent over items):
+//   warp 0       TMA producer (one lane), in both CTAs
+//   warp 1       TMEM allocator in both CTAs; MMA issuer (one lane) in the
+//                even CTA only
 //   warps 2..9   epilogue: warp w owns TMEM lanes 32*(w%4).. and the
-//                column half (w-2)/4 of the 256-column tile
-// Tiles: M=128 x N=256 per MMA instruction, K=16; TMEM X = cols 0..255,
-// Y = cols 256..511; a 2-stage 96 KB smem ring (A_hi, A_lo, B_hi, B_lo).
+//                column half (w-2)/4 of the 256-column tile, in both CTAs
+// TMEM accumulators X0 = cols 0..255, X1 = cols 256..511 in each CTA (its
+// 128 rows); a 3-stage 64 KB smem ring per CTA (A_hi, A_lo, B_hi, B_lo halves).
+// Barriers: a stage's "full" barrier lives in the even CTA and counts both
+// CTAs' bytes; "empty" and "accumulator ready" are signalled to both CTAs by
+// multicast commits; "accumulator drained" lives in the even CTA and counts
+// the epilogue warps of both.
 // Every mbarrier wait is bounded in time; on expiry the kernel records
 // LGB_ETIMEOUT in a device flag, drains what it issued and returns.
 #include <cuda.h>
@@ -43,28 +56,26 @@
 namespace lgb {
 namespace tc {
 
-constexpr int BM = 128, BN = 256, BK = 64, STAGES = 2;
+constexpr int BM = 128;                                    // A rows per CTA (256 per pair)
+constexpr int BN = 256;                                    // output columns per pair tile
+constexpr int BNC = BN / 2;                                // B rows held per CTA
+constexpr int BK = 64, STAGES = 3;
 constexpr int KSTEPS = BK / 16;                            // MMA k-steps per K block
-#ifndef LGB_KSUB
-#define LGB_KSUB 4
-#endif
-constexpr int KSUB = LGB_KSUB;                             // k-steps per hi.hi chain
-constexpr int CHUNKS = KSTEPS / KSUB;                      // X chunks per K block
 constexpr uint32_t A_BYTES = BM * BK * 2;                  // 16 KB per plane
-constexpr uint32_t B_BYTES = BN * BK * 2;                  // 32 KB per plane
-constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 96 KB
+constexpr uint32_t B_BYTES = BNC * BK * 2;                 // 16 KB per plane
+constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 64 KB per CTA
 constexpr uint32_t BAR_BYTES = 128;
-constexpr uint32_t SMEM_BYTES = STAGES * STAGE_BYTES + BAR_BYTES + 1024;
+constexpr uint32_t SMEM_BYTES = STAGES * STAGE_BYTES + BAR_BYTES + 8 * 4096 + 1024;
 constexpr int EPI_WARPS = 8;
 constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t X_COL = 0, Y_COL = 256;
+constexpr uint32_t ACC_COLS = 256;                         // one accumulator: 128 lanes x 256 fp32
 constexpr unsigned long long WAIT_NS = 2000000000ull;      // 2 s bound on any wait
 
 struct Params {
   int stage;                 // 1 or 2
   int kblocks;               // K / 64
-  int m_tiles, n_tiles;
+  int m_tiles, n_tiles;      // pair tiles: 256 A rows x 256 output columns
   int n_items;               // Q * m_tiles * n_tiles
   int L;
   uint32_t idesc;
@@ -135,10 +146,36 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* er
     }
   }
 }
+// Shared-memory address of the same variable in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t map_to_cta(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// arrive (+ expected bytes) on a barrier given by its cluster address
+__device__ __forceinline__ void mbar_expect_tx_cluster(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.release.cluster.shared::cluster.b64 _, [%0], %1;" ::"r"(bar),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// TMA tile load into this CTA's shared memory, completion counted on a
+// barrier of either CTA of the pair (cluster address).
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
                                             int x, int y, int z) {
   asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
       : "memory");
@@ -162,17 +199,23 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
   d |= (uint64_t)2 << 61;                             // 128-byte swizzle
   return d;
 }
+// D[256 x 256] (+)= A[256 x 16] . B[256 x 16]^T over the CTA pair: each CTA
+// supplies 128 rows of A and 128 rows of B at the same shared-memory offset.
 __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
                                         uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
       "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
+// arrive once on the barrier at this offset in both CTAs when the MMAs
+// issued so far have completed
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar) {
+  const uint16_t both = 3;
   asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;" ::"r"(bar), "h"(both)
       : "memory");
 }
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
@@ -229,19 +272,32 @@ __device__ __forceinline__ void drain_add(uint32_t taddr, float (&run)[128]) {
   }
 }
 
+// Output stores go through a 4 KB shared-memory slice per epilogue warp:
+// a warp holds 32 rows x (a few) 16-byte chunks per row in registers, one
+// row per lane; it writes them to the slice with the 16-byte chunk index
+// XOR-swizzled by row (no bank conflicts on either side) and reads them back
+// so that consecutive lanes cover consecutive chunks of the same row: one
+// warp store then covers 8 rows x 64 B (stage 1) or 4 rows x 128 B (stage 2)
+// instead of 32 rows x 16 B.
+constexpr uint32_t STG_BYTES = 4096;                       // per epilogue warp
+
+// Stage 1: G rows (split into hi/lo planes) = the stage-2 A operand.
+// A warp's 32 rows are 32 consecutive complex rows u with one plane half h.
 template <bool BF16>
 __device__ __forceinline__ void write_stage1(const Params& p, const Item& w, int row, int ch,
-                                             const float (&run)[128]) {
-  const int h = row >> 6, u = w.tm * 64 + (row & 63);
-  if (u >= p.M) return;
+                                             const float (&run)[128], uint8_t* stg) {
+  const int lane = row & 31;
+  const int h = row >> 6;
+  const int u0 = w.tm * 64 + (row & 63) - lane;            // first row of this warp
   const size_t K2 = 2 * (size_t)p.kp_out;
   const int c0 = w.tn * BN + ch * 128;
-  const size_t off = ((size_t)w.q * p.M + u) * K2 + (size_t)h * p.kp_out + c0;
+  uint16_t* const planes[2] = {p.g_hi, p.g_lo};
 #pragma unroll
   for (int cc = 0; cc < 4; ++cc) {
-    if (c0 + cc * 32 >= p.kp_out) break;
+    if (c0 + cc * 32 >= p.kp_out) break;                   // uniform over the warp
+    // registers -> slice: [plane][32 rows][4 chunks of 8 columns]
 #pragma unroll
-    for (int v8 = 0; v8 < 4; ++v8) {          // 8 columns -> one 16-byte store per plane
+    for (int v8 = 0; v8 < 4; ++v8) {
       uint32_t ph[4], pl[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
@@ -252,35 +308,70 @@ __device__ __forceinline__ void write_stage1(const Params& p, const Item& w, int
         ph[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
         pl[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
       }
-      *reinterpret_cast<uint4*>(p.g_hi + off + cc * 32 + v8 * 8) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
-      *reinterpret_cast<uint4*>(p.g_lo + off + cc * 32 + v8 * 8) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
+      const uint32_t slot = lane * 64 + ((v8 ^ ((lane >> 1) & 3)) << 4);
+      *reinterpret_cast<uint4*>(stg + slot) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
+      *reinterpret_cast<uint4*>(stg + 2048 + slot) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
     }
+    __syncwarp();
+    // slice -> global: lane j takes chunk (j & 3) of row 8t + (j >> 2)
+#pragma unroll
+    for (int pl = 0; pl < 2; ++pl) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int r = t * 8 + (lane >> 2), c = lane & 3;
+        const uint4 v = *reinterpret_cast<const uint4*>(stg + pl * 2048 + r * 64 +
+                                                        ((c ^ ((r >> 1) & 3)) << 4));
+        if (u0 + r < p.M)
+          *reinterpret_cast<uint4*>(planes[pl] + ((size_t)w.q * p.M + u0 + r) * K2 +
+                                    (size_t)h * p.kp_out + c0 + cc * 32 + c * 8) = v;
+      }
+    }
+    __syncwarp();
   }
 }
 
 // Stage 2 column layout of a 256-column tile: half ch holds output columns
 // v = tn*128 + ch*64 + j, real parts in [0, 64), imaginary in [64, 128).
 __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int row, int ch,
-                                             const float (&run)[128]) {
-  const int u = w.tm * BM + row;
-  if (u >= p.M) return;
+                                             const float (&run)[128], uint8_t* stg) {
+  const int lane = row & 31;
+  const int u = w.tm * BM + row, u0 = u - lane;
   const float sf = pow2_scale_for(p.maxabs[w.psf]);
   const int v0 = w.tn * 128 + ch * 64;
   if (p.epilogue == 0) {
     const float inv = 1.f / (sf * p.sG);
     const double wt = p.weights ? p.weights[(size_t)w.psf * p.L + w.lam] : 1.0;
     const float coef = (float)(wt * p.unit2[matrix_slot(p, w.lam)]) * inv * inv;
-    float* dst = p.wbuf + ((size_t)w.psf * p.M + u) * p.ldw + v0;
+    float* const dst0 = p.wbuf + ((size_t)w.psf * p.M + u0) * p.ldw + v0;
 #pragma unroll
-    for (int j = 0; j < 64; j += 4) {
-      if (v0 + j >= p.N) break;
-      float r[4];
+    for (int cc = 0; cc < 2; ++cc) {
+      if (v0 + cc * 32 >= p.N) break;                      // uniform over the warp
+      // registers -> slice: [32 rows][8 chunks of 4 columns]
 #pragma unroll
-      for (int e = 0; e < 4; ++e)
-        r[e] = coef * fmaf(run[j + e], run[j + e], run[64 + j + e] * run[64 + j + e]);
-      red_add_v4(dst + j, r[0], r[1], r[2], r[3]);
+      for (int c = 0; c < 8; ++c) {
+        float r4[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int j = cc * 32 + c * 4 + e;
+          r4[e] = coef * fmaf(run[j], run[j], run[64 + j] * run[64 + j]);
+        }
+        *reinterpret_cast<float4*>(stg + lane * 128 + ((c ^ (lane & 7)) << 4)) =
+            make_float4(r4[0], r4[1], r4[2], r4[3]);
+      }
+      __syncwarp();
+      // slice -> global: lane j takes chunk (j & 7) of row 4t + (j >> 3)
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int r = t * 4 + (lane >> 3), c = lane & 7;
+        const float4 v = *reinterpret_cast<const float4*>(stg + r * 128 + ((c ^ (r & 7)) << 4));
+        const int col = cc * 32 + c * 4;
+        if (u0 + r < p.M && v0 + col < p.N)
+          red_add_v4(dst0 + (size_t)r * p.ldw + col, v.x, v.y, v.z, v.w);
+      }
+      __syncwarp();
     }
   } else {
+    if (u >= p.M) return;
     const double scl = p.cscale / ((double)sf * (double)p.sG);
     double2* outc = reinterpret_cast<double2*>(p.out) + (size_t)u * p.N;
 #pragma unroll
@@ -300,37 +391,39 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
   const uint32_t base = (raw + 1023u) & ~1023u;
   uint8_t* const gbase = smem_raw + (base - raw);
   const uint32_t bars = base + STAGES * STAGE_BYTES;
-  auto full_bar = [&](int s) { return bars + 8u * s; };
-  auto empty_bar = [&](int s) { return bars + 16u + 8u * s; };
-  const uint32_t xf_bar = bars + 32u;    // X chunk ready       (MMA -> epilogue)
-  const uint32_t xe_bar = bars + 40u;    // X chunk drained     (epilogue -> MMA)
-  const uint32_t yf_bar = bars + 48u;    // Y ready (item end)  (MMA -> epilogue)
-  const uint32_t ye_bar = bars + 56u;    // Y drained           (epilogue -> MMA)
-  const uint32_t drain_bar = bars + 64u;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * STAGE_BYTES + 72);
+  auto full_bar = [&](int s) { return bars + 8u * s; };           // even CTA: both CTAs' bytes
+  auto empty_bar = [&](int s) { return bars + 32u + 8u * s; };    // both CTAs
+  auto acc_full = [&](int b) { return bars + 64u + 8u * b; };     // accumulator b ready, both CTAs
+  auto acc_empty = [&](int b) { return bars + 80u + 8u * b; };    // accumulator b drained, even CTA
+  const uint32_t drain_bar = bars + 96u;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * STAGE_BYTES + 112);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_rank();
+  const bool leader = rank == 0;
+  const int pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(full_bar(s), 1);
+      mbar_init(full_bar(s), 2);
       mbar_init(empty_bar(s), 1);
     }
-    mbar_init(xf_bar, 1);
-    mbar_init(xe_bar, EPI_WARPS);
-    mbar_init(yf_bar, 1);
-    mbar_init(ye_bar, EPI_WARPS);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(acc_full(b), 1);
+      mbar_init(acc_empty(b), 2 * EPI_WARPS);
+    }
     mbar_init(drain_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
                  "r"(TMEM_COLS));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
   }
   tc_fence_before();
   __syncthreads();
+  cluster_sync();                        // both CTAs' barriers and TMEM are ready
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
@@ -341,72 +434,60 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
       prefetch_map(&tmB_hi); prefetch_map(&tmB_lo);
       uint32_t it = 0;
       bool ok = true;
-      for (int i = blockIdx.x; ok && i < p.n_items; i += gridDim.x) {
+      for (int i = pair; ok && i < p.n_items; i += npairs) {
         const Item w = decode(p, i);
         // stage 1: A = E1 block of lam, B = f^T of q; stage 2: A = G of q, B = E2 block of lam
         const int az = p.stage == 1 ? matrix_slot(p, w.lam) : w.q;
         const int bz = p.stage == 1 ? w.q : matrix_slot(p, w.lam);
+        const int ay = (2 * w.tm + (int)rank) * BM;
+        const int by = w.tn * BN + (int)rank * BNC;
         for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
           const int s = it % STAGES;
           if (!mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1, p.err)) { ok = false; break; }
-          mbar_expect_tx(full_bar(s), STAGE_BYTES);
+          const uint32_t fb = map_to_cta(full_bar(s), 0);
+          mbar_expect_tx_cluster(fb, STAGE_BYTES);
           const uint32_t sa = base + s * STAGE_BYTES;
-          tma_load_3d(sa, &tmA_hi, full_bar(s), kb * BK, w.tm * BM, az);
-          tma_load_3d(sa + A_BYTES, &tmA_lo, full_bar(s), kb * BK, w.tm * BM, az);
-          tma_load_3d(sa + 2 * A_BYTES, &tmB_hi, full_bar(s), kb * BK, w.tn * BN, bz);
-          tma_load_3d(sa + 2 * A_BYTES + B_BYTES, &tmB_lo, full_bar(s), kb * BK, w.tn * BN, bz);
+          tma_load_3d(sa, &tmA_hi, fb, kb * BK, ay, az);
+          tma_load_3d(sa + A_BYTES, &tmA_lo, fb, kb * BK, ay, az);
+          tma_load_3d(sa + 2 * A_BYTES, &tmB_hi, fb, kb * BK, by, bz);
+          tma_load_3d(sa + 2 * A_BYTES + B_BYTES, &tmB_lo, fb, kb * BK, by, bz);
         }
       }
-      // every copy this thread issued has landed before the CTA exits
-      for (uint32_t k = (it > STAGES ? it - STAGES : 0); k < it; ++k)
-        mbar_wait(full_bar(k % STAGES), (k / STAGES) & 1, p.err);
+      // every copy of both CTAs has landed before the pair exits (the even
+      // CTA's full barriers count the odd CTA's bytes too)
+      if (leader)
+        for (uint32_t k = (it > STAGES ? it - STAGES : 0); k < it; ++k)
+          mbar_wait(full_bar(k % STAGES), (k / STAGES) & 1, p.err);
     }
   } else if (warp == 1) {
     // ------------------------------------------------------- MMA issuer
-    if (lane == 0) {
-      uint32_t it = 0, xc = 0, yi = 0;
+    if (leader && lane == 0) {
+      uint32_t it = 0;                       // K blocks issued (also accumulator uses)
       bool ok = true;
-      const uint32_t X = tmem + X_COL, Y = tmem + Y_COL;
-      for (int i = blockIdx.x; ok && i < p.n_items; i += gridDim.x, ++yi) {
-        for (int kb = 0; kb < p.kblocks && ok; ++kb, ++it) {
-          const int s = it % STAGES;
+      for (int i = pair; ok && i < p.n_items; i += npairs) {
+        for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
+          const int s = it % STAGES, xb = it & 1;
           if (!mbar_wait(full_bar(s), (it / STAGES) & 1, p.err)) { ok = false; break; }
+          // accumulator xb was drained by both CTAs (its previous block, it - 2)
+          if (!mbar_wait(acc_empty(xb), ((it >> 1) & 1) ^ 1, p.err)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t sa = base + s * STAGE_BYTES;
+          const uint32_t sa = base + s * STAGE_BYTES, X = tmem + xb * ACC_COLS;
 #pragma unroll
-          for (int c = 0; c < CHUNKS; ++c, ++xc) {
-            // X <- hi.hi over KSUB k-steps, once the previous chunk is drained
-            if (!mbar_wait(xe_bar, (xc & 1) ^ 1, p.err)) { ok = false; break; }
-            tc_fence_after();
-#pragma unroll
-            for (int kk = 0; kk < KSUB; ++kk) {
-              const int k = c * KSUB + kk;
-              mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32), p.idesc,
-                      kk ? 1u : 0u);
-            }
-            mma_commit(xf_bar);
-            // Y <- hi.lo + lo.hi (one chain per item, restarted after Y is drained)
-            const bool y_first = (kb == 0 && c == 0);
-            if (y_first) {
-              if (!mbar_wait(ye_bar, (yi & 1) ^ 1, p.err)) { ok = false; break; }
-              tc_fence_after();
-            }
-#pragma unroll
-            for (int kk = 0; kk < KSUB; ++kk) {
-              const int k = c * KSUB + kk;
-              mma_f16(Y, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + B_BYTES + k * 32),
-                      p.idesc, (y_first && kk == 0) ? 0u : 1u);
-              mma_f16(Y, smem_desc(sa + A_BYTES + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32),
-                      p.idesc, 1u);
-            }
+          for (int k = 0; k < KSTEPS; ++k) {     // hi.lo + lo.hi: small terms first
+            mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + B_BYTES + k * 32),
+                    p.idesc, k ? 1u : 0u);
+            mma_f16(X, smem_desc(sa + A_BYTES + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32),
+                    p.idesc, 1u);
           }
-          mma_commit(empty_bar(s));     // smem stage free once these MMAs retire
+#pragma unroll
+          for (int k = 0; k < KSTEPS; ++k)       // hi.hi last
+            mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32), p.idesc, 1u);
+          mma_commit_pair(empty_bar(s));         // both CTAs' stage s free once these retire
+          mma_commit_pair(acc_full(xb));         // accumulator xb ready for the epilogues
         }
-        if (!ok) break;
-        mma_commit(yf_bar);
       }
       // all issued MMAs have retired before TMEM is released
-      mma_commit(drain_bar);
+      mma_commit_pair(drain_bar);
       mbar_wait(drain_bar, 0, p.err);
     }
   } else {
@@ -415,43 +496,38 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
     const int ch = (warp - 2) >> 2;          // column half of the tile
     const int row = q4 * 32 + lane;
     const uint32_t trow = tmem + ((uint32_t)(q4 * 32) << 16) + ch * 128;
-    uint32_t xc = 0, yi = 0;
+    const uint32_t empty_lead[2] = {map_to_cta(acc_empty(0), 0), map_to_cta(acc_empty(1), 0)};
+    uint8_t* const stg = gbase + STAGES * STAGE_BYTES + BAR_BYTES + (warp - 2) * STG_BYTES;
+    uint32_t it = 0;
     bool ok = true;
-    for (int i = blockIdx.x; ok && i < p.n_items; i += gridDim.x, ++yi) {
-      const Item w = decode(p, i);
+    for (int i = pair; ok && i < p.n_items; i += npairs) {
+      Item w = decode(p, i);
+      w.tm = 2 * w.tm + (int)rank;           // this CTA's 128-row tile
       float run[128];
 #pragma unroll
       for (int j = 0; j < 128; ++j) run[j] = 0.f;
-      for (int kb = 0; kb < p.kblocks && ok; ++kb) {
-        for (int c = 0; c < CHUNKS; ++c, ++xc) {
-          ok = __all_sync(0xffffffffu, mbar_wait(xf_bar, xc & 1, p.err));
-          if (!ok) break;
-          tc_fence_after();
-          drain_add(trow + X_COL, run);
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(xe_bar);
-        }
+      for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
+        const int xb = it & 1;
+        ok = __all_sync(0xffffffffu, mbar_wait(acc_full(xb), (it >> 1) & 1, p.err));
+        if (!ok) break;
+        tc_fence_after();
+        drain_add(trow + xb * ACC_COLS, run);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive_cluster(empty_lead[xb]);
       }
       if (!ok) break;
-      ok = __all_sync(0xffffffffu, mbar_wait(yf_bar, yi & 1, p.err));
-      if (!ok) break;
-      tc_fence_after();
-      drain_add(trow + Y_COL, run);
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(ye_bar);
-      if (p.stage == 1) write_stage1<BF16>(p, w, row, ch, run);
-      else write_stage2(p, w, row, ch, run);
+      if (p.stage == 1) write_stage1<BF16>(p, w, row, ch, run, stg);
+      else write_stage2(p, w, row, ch, run, stg);
     }
   }
 
   tc_fence_before();
   __syncthreads();
+  cluster_sync();                        // no CTA leaves while its pair may still use it
   if (warp == 1) {
-    __syncwarp();
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
   }
 }
 
@@ -494,8 +570,24 @@ constexpr uint32_t make_idesc(bool bf16) {
   return (1u << 4)                          // D format: FP32
          | ((bf16 ? 1u : 0u) << 7)          // A format: BF16 (1) / FP16 (0)
          | ((bf16 ? 1u : 0u) << 10)         // B format
-         | ((uint32_t)(BN >> 3) << 17)      // N
-         | ((uint32_t)(BM >> 4) << 24);     // M
+         | ((uint32_t)(BN >> 3) << 17)      // N = 256
+         | ((uint32_t)((2 * BM) >> 4) << 24);  // M = 256 (the CTA pair)
+}
+
+// Largest number of CTA pairs of this kernel resident at once (per device).
+template <bool BF16>
+static int max_pairs(cudaLaunchConfig_t& cfg) {
+  static std::mutex mu;
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  std::lock_guard<std::mutex> lock(mu);
+  if (cached[dev] == 0) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, split_mft_kernel<BF16>, &cfg) != cudaSuccess) n = 0;
+    cached[dev] = n;
+  }
+  return cached[dev];
 }
 
 template <bool BF16>
@@ -509,9 +601,22 @@ static int launch_one(const Params& p, const CUtensorMap& a_hi, const CUtensorMa
   });
   LGB_CUDA(attr_err);
   if (p.n_items <= 0) return LGB_OK;
-  const int grid = std::min(p.n_items, sm_count());
-  split_mft_kernel<BF16><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(a_hi, a_lo, b_hi, b_lo, p);
-  LGB_CUDA(cudaGetLastError());
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2);
+  cfg.blockDim = dim3(NUM_THREADS);
+  cfg.dynamicSmemBytes = SMEM_BYTES;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const int pairs = max_pairs<BF16>(cfg);
+  LGB_REQUIRE(pairs > 0, LGB_ECUDA, "split mft: no CTA pair of the tensor-core kernel fits on this GPU");
+  cfg.gridDim = dim3(2 * std::min(p.n_items, pairs));
+  LGB_CUDA(cudaLaunchKernelEx(&cfg, split_mft_kernel<BF16>, a_hi, a_lo, b_hi, b_lo, p));
   return LGB_OK;
 }
 
@@ -538,12 +643,12 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   const int Lm = q.lam_idx ? q.L_bank : q.L;     // DFT-matrix slots held
   if ((st = make_map(&a_hi, q.e1_hi, q.bf16, 2 * q.kp1, mrows1, Lm, BM))) return st;
   if ((st = make_map(&a_lo, q.e1_lo, q.bf16, 2 * q.kp1, mrows1, Lm, BM))) return st;
-  if ((st = make_map(&b_hi, q.f_hi, q.bf16, 2 * q.kp1, q.n, Q, BN))) return st;
-  if ((st = make_map(&b_lo, q.f_lo, q.bf16, 2 * q.kp1, q.n, Q, BN))) return st;
+  if ((st = make_map(&b_hi, q.f_hi, q.bf16, 2 * q.kp1, q.n, Q, BNC))) return st;
+  if ((st = make_map(&b_lo, q.f_lo, q.bf16, 2 * q.kp1, q.n, Q, BNC))) return st;
   Params p{};
   p.stage = 1;
   p.kblocks = 2 * q.kp1 / BK;
-  p.m_tiles = cdiv(q.M, 64);
+  p.m_tiles = cdiv(cdiv(q.M, 64), 2);          // pairs of 64-row (128 block-row) E1 tiles
   p.n_tiles = cdiv(q.kp2, BN);
   p.n_items = Q * p.m_tiles * p.n_tiles;
   p.L = q.L;
@@ -564,11 +669,11 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   // ---- stage 2: F = G . E2 (+ epilogue)
   if ((st = make_map(&a_hi, q.g_hi, q.bf16, 2 * q.kp2, q.M, Q, BM))) return st;
   if ((st = make_map(&a_lo, q.g_lo, q.bf16, 2 * q.kp2, q.M, Q, BM))) return st;
-  if ((st = make_map(&b_hi, q.e2_hi, q.bf16, 2 * q.kp2, nrows2, Lm, BN))) return st;
-  if ((st = make_map(&b_lo, q.e2_lo, q.bf16, 2 * q.kp2, nrows2, Lm, BN))) return st;
+  if ((st = make_map(&b_hi, q.e2_hi, q.bf16, 2 * q.kp2, nrows2, Lm, BNC))) return st;
+  if ((st = make_map(&b_lo, q.e2_lo, q.bf16, 2 * q.kp2, nrows2, Lm, BNC))) return st;
   p.stage = 2;
   p.kblocks = 2 * q.kp2 / BK;
-  p.m_tiles = cdiv(q.M, BM);
+  p.m_tiles = cdiv(q.M, 2 * BM);
   p.n_tiles = cdiv(q.N, 128);
   p.n_items = Q * p.m_tiles * p.n_tiles;
   p.epilogue = q.epilogue;

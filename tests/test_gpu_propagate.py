@@ -29,7 +29,7 @@ def test_propagate_fp64_golden(golden, cuda_device, name):
 
 # split tolerances: two 16-bit planes give 16 (bf16) or 22 (fp16) significant
 # bits per operand, and the FP32 tensor-core accumulation is folded into
-# round-to-nearest registers every two MMA k-steps
+# round-to-nearest registers after every 64-wide K block
 SPLIT_TOL = {'split-bf16': 3e-5, 'split-fp16': 2e-6}
 
 
