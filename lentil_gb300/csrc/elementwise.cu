@@ -64,25 +64,30 @@ int launch_phasor_batch_c128(const double* amp, const double* opd, int H, int W,
 // K2s: split 16-bit transposed field operand.
 // Output row c (field column), K index r (field row) for the real part and
 // kp + r for the imaginary part: f^T in the stage-1 B-operand layout.
-// One block = 64 field rows x 32 field columns, looping over wavelengths.
+// One block = 64 field rows x 32 field columns and a contiguous group of
+// wavelengths (blockIdx.z = PSF * groups + group): splitting the wavelength
+// loop over blocks keeps enough blocks in flight to cover HBM latency.  The
+// transpose tile is double-buffered, so each wavelength needs one barrier.
 // ---------------------------------------------------------------------------
 constexpr int TR = 64, TC = 32, TPAD = 8;
 
 template <bool BF16, bool PHASOR>
-__global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a) {
-  __shared__ __align__(16) uint16_t tile[4][TC][TR + TPAD];   // re_hi, re_lo, im_hi, im_lo
+__global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, int groups) {
+  __shared__ __align__(16) uint16_t tile[2][4][TC][TR + TPAD];   // re_hi, re_lo, im_hi, im_lo
   const int tid = threadIdx.x;
   const int rt = blockIdx.x * TR, ct = blockIdx.y * TC;
-  const int b = blockIdx.z;                         // PSF
+  const int b = blockIdx.z / groups, g = blockIdx.z - b * groups;   // PSF, wavelength group
   const float sf = pow2_scale_for(a.maxabs[b]);
 
-  // load 8 pixels per thread once (coalesced along the field columns)
+  // thread (w, lane) owns field column ct + lane and rows rt + 8w .. 8w+7:
+  // each global load instruction reads 32 consecutive columns of one row,
+  // and the thread's 8 values of a plane are one 16-byte shared store
+  const int lane = tid & 31, w = tid >> 5;
   float amp_r[8], o_hi[8], o_lo[8];
   float2 fv[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    const int p = tid + 256 * k, rl = p >> 5, cl = p & 31;
-    const int r = rt + rl, c = ct + cl;
+    const int r = rt + 8 * w + k, c = ct + lane;
     amp_r[k] = 0.f; o_hi[k] = 0.f; o_lo[k] = 0.f; fv[k] = make_float2(0.f, 0.f);
     if (r < a.m && c < a.n) {
       if (PHASOR) {
@@ -99,7 +104,9 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a) {
   }
 
   const int L = PHASOR ? a.L : 1;
-  for (int l = 0; l < L; ++l) {
+  const int per = (L + groups - 1) / groups;
+  const int l0 = g * per, l1 = min(L, l0 + per);
+  for (int l = l0; l < l1; ++l) {
     if (PHASOR) {
       const float2 kk = a.khalf[a.lam_idx ? a.lam_idx[l] : l];   // 2/lambda, float-float pair
 #pragma unroll
@@ -114,16 +121,26 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a) {
         fv[k] = make_float2(amp_r[k] * cs, amp_r[k] * sn);
       }
     }
-    __syncthreads();   // previous wavelength's tile fully written out
+    uint32_t pk[4][4];                               // [plane][pair of rows]
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int p = tid + 256 * k, rl = p >> 5, cl = p & 31;
-      uint16_t h, lo;
-      Split16<BF16>::split(fv[k].x, h, lo);
-      tile[0][cl][rl] = h; tile[1][cl][rl] = lo;
-      Split16<BF16>::split(fv[k].y, h, lo);
-      tile[2][cl][rl] = h; tile[3][cl][rl] = lo;
+    for (int j = 0; j < 4; ++j) {
+      uint16_t rh0, rl0, ih0, il0, rh1, rl1, ih1, il1;
+      Split16<BF16>::split(fv[2 * j].x, rh0, rl0);
+      Split16<BF16>::split(fv[2 * j].y, ih0, il0);
+      Split16<BF16>::split(fv[2 * j + 1].x, rh1, rl1);
+      Split16<BF16>::split(fv[2 * j + 1].y, ih1, il1);
+      pk[0][j] = (uint32_t)rh0 | ((uint32_t)rh1 << 16);
+      pk[1][j] = (uint32_t)rl0 | ((uint32_t)rl1 << 16);
+      pk[2][j] = (uint32_t)ih0 | ((uint32_t)ih1 << 16);
+      pk[3][j] = (uint32_t)il0 | ((uint32_t)il1 << 16);
     }
+    // buffer l&1 was last read two wavelengths ago, before the barrier of the
+    // previous wavelength; row pitch 144 B keeps 8 lanes' 16-byte stores on
+    // distinct banks
+    uint16_t (*t)[TC][TR + TPAD] = tile[l & 1];
+#pragma unroll
+    for (int pl = 0; pl < 4; ++pl)
+      *reinterpret_cast<uint4*>(&t[pl][lane][8 * w]) = make_uint4(pk[pl][0], pk[pl][1], pk[pl][2], pk[pl][3]);
     __syncthreads();
     const size_t q = (size_t)b * L + l;
     const size_t K = 2 * (size_t)a.kp;
@@ -135,20 +152,28 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a) {
       if (c < a.n && r < a.kp) {
         uint16_t* dst = (plane & 1) ? a.lo : a.hi;
         const size_t off = (q * a.n + c) * K + ((plane >> 1) ? a.kp : 0) + r;
-        *reinterpret_cast<uint4*>(dst + off) = *reinterpret_cast<const uint4*>(&tile[plane][cl][seg * 8]);
+        *reinterpret_cast<uint4*>(dst + off) = *reinterpret_cast<const uint4*>(&t[plane][cl][seg * 8]);
       }
     }
   }
 }
 
 int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
-  dim3 grid(cdiv(a.kp, TR), cdiv(a.n, TC), a.amp ? a.batch : 1);
+  const int spatial = cdiv(a.kp, TR) * cdiv(a.n, TC);
+  const int psfs = a.amp ? a.batch : 1;
+  const int L = a.amp ? a.L : 1;
+  // enough blocks for ~8 resident per SM, no group smaller than one wavelength
+  int groups = cdiv(8 * sm_count(), std::max(1, spatial * psfs));
+  groups = std::max(1, std::min(groups, L));
+  groups = cdiv(L, cdiv(L, groups));                 // no empty trailing group
+  LGB_REQUIRE((long long)psfs * groups <= 65535, LGB_EINVAL, "split field: too many PSFs in one launch");
+  dim3 grid(cdiv(a.kp, TR), cdiv(a.n, TC), psfs * groups);
   if (a.amp) {
-    if (bf16) split_field_T_kernel<true, true><<<grid, 256, 0, s>>>(a);
-    else split_field_T_kernel<false, true><<<grid, 256, 0, s>>>(a);
+    if (bf16) split_field_T_kernel<true, true><<<grid, 256, 0, s>>>(a, groups);
+    else split_field_T_kernel<false, true><<<grid, 256, 0, s>>>(a, groups);
   } else {
-    if (bf16) split_field_T_kernel<true, false><<<grid, 256, 0, s>>>(a);
-    else split_field_T_kernel<false, false><<<grid, 256, 0, s>>>(a);
+    if (bf16) split_field_T_kernel<true, false><<<grid, 256, 0, s>>>(a, groups);
+    else split_field_T_kernel<false, false><<<grid, 256, 0, s>>>(a, groups);
   }
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
