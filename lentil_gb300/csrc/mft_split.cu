@@ -161,14 +161,19 @@ __device__ __forceinline__ void cluster_sync() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
                "barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
-// arrive (+ expected bytes) on a barrier given by its cluster address
+// arrive (+ expected bytes) on a barrier given by its cluster address.
+// Default (CTA-scope release) semantics: what these arrivals publish needs no
+// cluster-wide fence -- the producer has written nothing the consumer reads,
+// and an epilogue's TMEM reads are complete at tcgen05.wait::ld, ordered
+// against the next MMA by the tcgen05 fences around the barrier.  (A
+// cluster-scope release here stalled every epilogue warp on a memory barrier
+// once per K block: measured 11 % of the whole step.)
 __device__ __forceinline__ void mbar_expect_tx_cluster(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.release.cluster.shared::cluster.b64 _, [%0], %1;" ::"r"(bar),
-               "r"(bytes)
+  asm volatile("mbarrier.arrive.expect_tx.shared::cluster.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
                : "memory");
 }
 __device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar) : "memory");
+  asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 // TMA tile load into this CTA's shared memory, completion counted on a
 // barrier of either CTA of the pair (cluster address).
