@@ -65,7 +65,7 @@ constexpr uint32_t A_BYTES = BM * BK * 2;                  // 16 KB per plane
 constexpr uint32_t B_BYTES = BNC * BK * 2;                 // 16 KB per plane
 constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 64 KB per CTA
 constexpr uint32_t BAR_BYTES = 128;
-constexpr uint32_t SMEM_BYTES = STAGES * STAGE_BYTES + BAR_BYTES + 8 * 4096 + 1024;
+constexpr uint32_t SMEM_BYTES = STAGES * STAGE_BYTES + 8 * 4096 + BAR_BYTES + 1024;
 constexpr int EPI_WARPS = 8;
 constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
 constexpr uint32_t TMEM_COLS = 512;
@@ -185,6 +185,32 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
       : "memory");
 }
+// Bulk tensor store / FP32 reduce-add of a swizzled shared-memory tile
+// (async proxy; completion tracked by bulk groups of the issuing thread).
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, uint32_t src, int x, int y, int z) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(src), "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void tma_reduce_add_3d(const CUtensorMap* map, uint32_t src, int x, int y,
+                                                  int z) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(src), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the shared-memory sources of this thread's bulk groups may be overwritten
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+// this thread's bulk groups have completed their global writes
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 __device__ __forceinline__ void prefetch_map(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
@@ -277,30 +303,34 @@ __device__ __forceinline__ void drain_add(uint32_t taddr, float (&run)[128]) {
   }
 }
 
-// Output stores go through a 4 KB shared-memory slice per epilogue warp:
-// a warp holds 32 rows x (a few) 16-byte chunks per row in registers, one
-// row per lane; it writes them to the slice with the 16-byte chunk index
-// XOR-swizzled by row (no bank conflicts on either side) and reads them back
-// so that consecutive lanes cover consecutive chunks of the same row: one
-// warp store then covers 8 rows x 64 B (stage 1) or 4 rows x 128 B (stage 2)
-// instead of 32 rows x 16 B.
+// Output stores go through a 4 KB shared-memory slice per epilogue warp
+// (1024-byte aligned): the warp writes its 32 rows (one per lane) of 16-byte
+// chunks into the slice in the swizzled layout of a TMA box (16-byte chunk
+// index XOR-ed with the row bits, which also keeps both the writes and the
+// TMA read free of bank conflicts), and one lane hands the box to a bulk
+// tensor store (stage 1) or FP32 bulk reduce-add (stage 2).  The copies run
+// asynchronously; the warp returns to draining the next item and waits for
+// the TMA to have read the slice only before it rewrites it.  TMA clips the
+// rows past M and the columns past the tensor's extent.
 constexpr uint32_t STG_BYTES = 4096;                       // per epilogue warp
 
-// Stage 1: G rows (split into hi/lo planes) = the stage-2 A operand.
-// A warp's 32 rows are 32 consecutive complex rows u with one plane half h.
+// Stage 1: G rows (split into hi/lo planes) = the stage-2 A operand, as two
+// 32 x 32 boxes (64-byte rows, 64-byte swizzle) per pass.  A warp's 32 rows
+// are 32 consecutive complex rows u with one plane half h.
 template <bool BF16>
 __device__ __forceinline__ void write_stage1(const Params& p, const Item& w, int row, int ch,
-                                             const float (&run)[128], uint8_t* stg) {
+                                             const float (&run)[128], uint8_t* stg,
+                                             const CUtensorMap* map_hi, const CUtensorMap* map_lo) {
   const int lane = row & 31;
   const int h = row >> 6;
   const int u0 = w.tm * 64 + (row & 63) - lane;            // first row of this warp
-  const size_t K2 = 2 * (size_t)p.kp_out;
   const int c0 = w.tn * BN + ch * 128;
-  uint16_t* const planes[2] = {p.g_hi, p.g_lo};
+  const uint32_t s_hi = smem_u32(stg), s_lo = s_hi + 2048;
 #pragma unroll
   for (int cc = 0; cc < 4; ++cc) {
     if (c0 + cc * 32 >= p.kp_out) break;                   // uniform over the warp
-    // registers -> slice: [plane][32 rows][4 chunks of 8 columns]
+    if (lane == 0) bulk_wait_read();                       // previous box read out of the slice
+    __syncwarp();
 #pragma unroll
     for (int v8 = 0; v8 < 4; ++v8) {
       uint32_t ph[4], pl[4];
@@ -317,28 +347,24 @@ __device__ __forceinline__ void write_stage1(const Params& p, const Item& w, int
       *reinterpret_cast<uint4*>(stg + slot) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
       *reinterpret_cast<uint4*>(stg + 2048 + slot) = make_uint4(pl[0], pl[1], pl[2], pl[3]);
     }
+    fence_async_smem();
     __syncwarp();
-    // slice -> global: lane j takes chunk (j & 3) of row 8t + (j >> 2)
-#pragma unroll
-    for (int pl = 0; pl < 2; ++pl) {
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int r = t * 8 + (lane >> 2), c = lane & 3;
-        const uint4 v = *reinterpret_cast<const uint4*>(stg + pl * 2048 + r * 64 +
-                                                        ((c ^ ((r >> 1) & 3)) << 4));
-        if (u0 + r < p.M)
-          *reinterpret_cast<uint4*>(planes[pl] + ((size_t)w.q * p.M + u0 + r) * K2 +
-                                    (size_t)h * p.kp_out + c0 + cc * 32 + c * 8) = v;
-      }
+    if (lane == 0) {
+      const int x = h * p.kp_out + c0 + cc * 32;
+      tma_store_3d(map_hi, s_hi, x, u0, w.q);
+      tma_store_3d(map_lo, s_lo, x, u0, w.q);
+      bulk_commit();
     }
-    __syncwarp();
   }
 }
 
 // Stage 2 column layout of a 256-column tile: half ch holds output columns
 // v = tn*128 + ch*64 + j, real parts in [0, 64), imaginary in [64, 128).
+// Intensity: two 32 x 32 FP32 boxes (128-byte rows, 128-byte swizzle)
+// reduce-added into the window.
 __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int row, int ch,
-                                             const float (&run)[128], uint8_t* stg) {
+                                             const float (&run)[128], uint8_t* stg,
+                                             const CUtensorMap* map_w) {
   const int lane = row & 31;
   const int u = w.tm * BM + row, u0 = u - lane;
   const float sf = pow2_scale_for(p.maxabs[w.psf]);
@@ -347,11 +373,12 @@ __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int
     const float inv = 1.f / (sf * p.sG);
     const double wt = p.weights ? p.weights[(size_t)w.psf * p.L + w.lam] : 1.0;
     const float coef = (float)(wt * p.unit2[matrix_slot(p, w.lam)]) * inv * inv;
-    float* const dst0 = p.wbuf + ((size_t)w.psf * p.M + u0) * p.ldw + v0;
+    const uint32_t s0 = smem_u32(stg);
 #pragma unroll
     for (int cc = 0; cc < 2; ++cc) {
       if (v0 + cc * 32 >= p.N) break;                      // uniform over the warp
-      // registers -> slice: [32 rows][8 chunks of 4 columns]
+      if (lane == 0) bulk_wait_read();
+      __syncwarp();
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
         float r4[4];
@@ -363,17 +390,12 @@ __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int
         *reinterpret_cast<float4*>(stg + lane * 128 + ((c ^ (lane & 7)) << 4)) =
             make_float4(r4[0], r4[1], r4[2], r4[3]);
       }
+      fence_async_smem();
       __syncwarp();
-      // slice -> global: lane j takes chunk (j & 7) of row 4t + (j >> 3)
-#pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        const int r = t * 4 + (lane >> 3), c = lane & 7;
-        const float4 v = *reinterpret_cast<const float4*>(stg + r * 128 + ((c ^ (r & 7)) << 4));
-        const int col = cc * 32 + c * 4;
-        if (u0 + r < p.M && v0 + col < p.N)
-          red_add_v4(dst0 + (size_t)r * p.ldw + col, v.x, v.y, v.z, v.w);
+      if (lane == 0) {
+        tma_reduce_add_3d(map_w, s0, v0 + cc * 32, u0, w.psf);
+        bulk_commit();
       }
-      __syncwarp();
     }
   } else {
     if (u >= p.M) return;
@@ -390,18 +412,19 @@ template <bool BF16>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
                  const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo,
+                 const __grid_constant__ CUtensorMap tmC0, const __grid_constant__ CUtensorMap tmC1,
                  const Params p) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
   uint8_t* const gbase = smem_raw + (base - raw);
-  const uint32_t bars = base + STAGES * STAGE_BYTES;
+  const uint32_t bars = base + STAGES * STAGE_BYTES + EPI_WARPS * STG_BYTES;
   auto full_bar = [&](int s) { return bars + 8u * s; };           // even CTA: both CTAs' bytes
   auto empty_bar = [&](int s) { return bars + 32u + 8u * s; };    // both CTAs
   auto acc_full = [&](int b) { return bars + 64u + 8u * b; };     // accumulator b ready, both CTAs
   auto acc_empty = [&](int b) { return bars + 80u + 8u * b; };    // accumulator b drained, even CTA
   const uint32_t drain_bar = bars + 96u;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + STAGES * STAGE_BYTES + 112);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + (bars - base) + 112);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t rank = cluster_rank();
@@ -502,7 +525,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
     const int row = q4 * 32 + lane;
     const uint32_t trow = tmem + ((uint32_t)(q4 * 32) << 16) + ch * 128;
     const uint32_t empty_lead[2] = {map_to_cta(acc_empty(0), 0), map_to_cta(acc_empty(1), 0)};
-    uint8_t* const stg = gbase + STAGES * STAGE_BYTES + BAR_BYTES + (warp - 2) * STG_BYTES;
+    uint8_t* const stg = gbase + STAGES * STAGE_BYTES + (warp - 2) * STG_BYTES;
     uint32_t it = 0;
     bool ok = true;
     for (int i = pair; ok && i < p.n_items; i += npairs) {
@@ -522,9 +545,11 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
         if (lane == 0) mbar_arrive_cluster(empty_lead[xb]);
       }
       if (!ok) break;
-      if (p.stage == 1) write_stage1<BF16>(p, w, row, ch, run, stg);
-      else write_stage2(p, w, row, ch, run, stg);
+      if (p.stage == 1) write_stage1<BF16>(p, w, row, ch, run, stg, &tmC0, &tmC1);
+      else write_stage2(p, w, row, ch, run, stg, &tmC0);
     }
+    // the bulk stores / reduce-adds this warp issued have landed
+    if (lane == 0) bulk_wait_all();
   }
 
   tc_fence_before();
@@ -551,24 +576,36 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3-D K-major operand map: dims {K, rows, batch}, box {64, box_rows, 1}.
-static int make_map(CUtensorMap* map, const void* ptr, bool bf16, int K, int rows, int batch,
-                    int box_rows) {
+// 3-D row-major map: dims {K, rows, batch} of elem_bytes-wide elements, box
+// {box_k, box_rows, 1}.
+static int make_map_any(CUtensorMap* map, const void* ptr, CUtensorMapDataType dtype, int elem_bytes,
+                        int K, int rows, int batch, int box_k, int box_rows, CUtensorMapSwizzle swz) {
   auto enc = encode_fn();
   LGB_REQUIRE(enc, LGB_ECUDA, "cuTensorMapEncodeTiled is unavailable");
   LGB_REQUIRE(((uintptr_t)ptr & 15) == 0, LGB_EINVAL, "tensor map base must be 16-byte aligned");
-  LGB_REQUIRE(K % BK == 0, LGB_EINVAL, "tensor map K must be a multiple of 64");
+  LGB_REQUIRE(((size_t)K * elem_bytes) % 16 == 0, LGB_EINVAL, "tensor map row pitch must be a multiple of 16 bytes");
   cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)batch};
-  cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)K * 2 * rows};
-  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+  cuuint64_t strides[2] = {(cuuint64_t)K * elem_bytes, (cuuint64_t)K * elem_bytes * rows};
+  cuuint32_t box[3] = {(cuuint32_t)box_k, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
-  CUresult res = enc(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
-                     3, const_cast<void*>(ptr), dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  CUresult res = enc(map, dtype, 3, const_cast<void*>(ptr), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (res != CUDA_SUCCESS)
     return set_error(LGB_ECUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)res));
   return LGB_OK;
+}
+
+static CUtensorMapDataType half_type(bool bf16) {
+  return bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+}
+
+// K-major 16-bit MMA operand: box {64, box_rows}, 128-byte swizzle.
+static int make_map(CUtensorMap* map, const void* ptr, bool bf16, int K, int rows, int batch,
+                    int box_rows) {
+  LGB_REQUIRE(K % BK == 0, LGB_EINVAL, "tensor map K must be a multiple of 64");
+  return make_map_any(map, ptr, half_type(bf16), 2, K, rows, batch, BK, box_rows,
+                      CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 constexpr uint32_t make_idesc(bool bf16) {
@@ -597,7 +634,8 @@ static int max_pairs(cudaLaunchConfig_t& cfg) {
 
 template <bool BF16>
 static int launch_one(const Params& p, const CUtensorMap& a_hi, const CUtensorMap& a_lo,
-                      const CUtensorMap& b_hi, const CUtensorMap& b_lo, cudaStream_t s) {
+                      const CUtensorMap& b_hi, const CUtensorMap& b_lo, const CUtensorMap& c0,
+                      const CUtensorMap& c1, cudaStream_t s) {
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
@@ -621,7 +659,7 @@ static int launch_one(const Params& p, const CUtensorMap& a_hi, const CUtensorMa
   const int pairs = max_pairs<BF16>(cfg);
   LGB_REQUIRE(pairs > 0, LGB_ECUDA, "split mft: no CTA pair of the tensor-core kernel fits on this GPU");
   cfg.gridDim = dim3(2 * std::min(p.n_items, pairs));
-  LGB_CUDA(cudaLaunchKernelEx(&cfg, split_mft_kernel<BF16>, a_hi, a_lo, b_hi, b_lo, p));
+  LGB_CUDA(cudaLaunchKernelEx(&cfg, split_mft_kernel<BF16>, a_hi, a_lo, b_hi, b_lo, c0, c1, p));
   return LGB_OK;
 }
 
@@ -641,7 +679,7 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   const int mrows1 = cdiv(q.M, 64) * 128;      // E1 block rows
   const int nrows2 = cdiv(q.N, 128) * 256;     // E2 block rows
   const uint32_t idesc = make_idesc(q.bf16);
-  CUtensorMap a_hi, a_lo, b_hi, b_lo;
+  CUtensorMap a_hi, a_lo, b_hi, b_lo, c0, c1;
   int st;
 
   // ---- stage 1: G = E1 . f
@@ -650,6 +688,12 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   if ((st = make_map(&a_lo, q.e1_lo, q.bf16, 2 * q.kp1, mrows1, Lm, BM))) return st;
   if ((st = make_map(&b_hi, q.f_hi, q.bf16, 2 * q.kp1, q.n, Q, BNC))) return st;
   if ((st = make_map(&b_lo, q.f_lo, q.bf16, 2 * q.kp1, q.n, Q, BNC))) return st;
+  if ((st = make_map_any(&c0, q.g_hi, half_type(q.bf16), 2, 2 * q.kp2, q.M, Q, 32, 32,
+                         CU_TENSOR_MAP_SWIZZLE_64B)))
+    return st;
+  if ((st = make_map_any(&c1, q.g_lo, half_type(q.bf16), 2, 2 * q.kp2, q.M, Q, 32, 32,
+                         CU_TENSOR_MAP_SWIZZLE_64B)))
+    return st;
   Params p{};
   p.stage = 1;
   p.kblocks = 2 * q.kp1 / BK;
@@ -666,8 +710,8 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   p.err = q.err;
   p.lam_idx = q.lam_idx;
   if (q.events) LGB_CUDA(cudaEventRecord(q.events[0], s));
-  st = q.bf16 ? launch_one<true>(p, a_hi, a_lo, b_hi, b_lo, s)
-              : launch_one<false>(p, a_hi, a_lo, b_hi, b_lo, s);
+  st = q.bf16 ? launch_one<true>(p, a_hi, a_lo, b_hi, b_lo, c0, c1, s)
+              : launch_one<false>(p, a_hi, a_lo, b_hi, b_lo, c0, c1, s);
   if (st) return st;
   if (q.events) LGB_CUDA(cudaEventRecord(q.events[1], s));
 
@@ -676,6 +720,12 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   if ((st = make_map(&a_lo, q.g_lo, q.bf16, 2 * q.kp2, q.M, Q, BM))) return st;
   if ((st = make_map(&b_hi, q.e2_hi, q.bf16, 2 * q.kp2, nrows2, Lm, BNC))) return st;
   if ((st = make_map(&b_lo, q.e2_lo, q.bf16, 2 * q.kp2, nrows2, Lm, BNC))) return st;
+  if (q.epilogue == 0) {
+    LGB_REQUIRE(q.ldw % 4 == 0, LGB_EINVAL, "split mft: intensity window pitch must be a multiple of 4");
+    if ((st = make_map_any(&c0, q.wbuf, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, q.ldw, q.M, q.batch, 32, 32,
+                           CU_TENSOR_MAP_SWIZZLE_128B)))
+      return st;
+  }
   p.stage = 2;
   p.kblocks = 2 * q.kp2 / BK;
   p.m_tiles = cdiv(q.M, 2 * BM);
@@ -689,8 +739,8 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   p.out = q.out;
   p.cscale = q.complex_scale;
   if (q.events) LGB_CUDA(cudaEventRecord(q.events[2], s));
-  st = q.bf16 ? launch_one<true>(p, a_hi, a_lo, b_hi, b_lo, s)
-              : launch_one<false>(p, a_hi, a_lo, b_hi, b_lo, s);
+  st = q.bf16 ? launch_one<true>(p, a_hi, a_lo, b_hi, b_lo, c0, c1, s)
+              : launch_one<false>(p, a_hi, a_lo, b_hi, b_lo, c0, c1, s);
   if (st) return st;
   if (q.events) LGB_CUDA(cudaEventRecord(q.events[3], s));
   return LGB_OK;
