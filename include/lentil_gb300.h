@@ -180,7 +180,7 @@ int lgb_phasor_adjoint(const lgb_c128* q, const lgb_c128* f, int m, int n, doubl
  *   for lam, w: img = propagate_dft(Wavefront(lam) * pupil, ...).insert(img, w)
  * (docs/user/performance.rst:44-49) fused for a batch of PSFs that share the
  * optics: phasor (lentil/plane.py:502-507), propagate_dft's MFT into its
- * output window (lentil/propagate.py:345-440 with lentil/fourier.py:5-103),
+ * output window (lentil/propagate.py:147-242 with lentil/fourier.py:5-103),
  * and the weighted |E|^2 overlap-add of Wavefront.insert
  * (lentil/wavefront.py:145-165, lentil/field.py:231-305).
  *

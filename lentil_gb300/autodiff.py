@@ -26,7 +26,7 @@ Geometry = namedtuple('Geometry', 'wavelength alpha shape shift offset slc plane
 def geometry(amp, wavelength, pixelscale_in, focal_length, pixelscale_out, shape,
              oversample=2, precision='fp64'):
     """MFT geometry of ``propagate_dft`` for an untilted single-field pupil
-    whose support is ``amp != 0`` (lentil/propagate.py:373-438,
+    whose support is ``amp != 0`` (lentil/propagate.py:175-240,
     lentil/plane.py:494-510): full output window, zero shift, slice offset."""
     a = dv.to_host(amp) if dv.is_tensor(amp) else np.asarray(amp)
     slc = util.boundary_slice(a != 0)

@@ -224,7 +224,7 @@ class Geometry:
 
 def plan_geometry(plane_shape, s, tilts, dx, focal_length, ptype, wavelengths, du, shape=None,
                   prop_shape=None, oversample=2, mask=None):
-    """Window maths of propagate_dft (lentil/propagate.py:373-438) for one
+    """Window maths of propagate_dft (lentil/propagate.py:175-240) for one
     field slice ``s`` of the pupil plane and every wavelength; wavelengths
     whose window misses the output are dropped (``keep`` lists the rest)."""
     off = util.slice_offset(s, plane_shape)

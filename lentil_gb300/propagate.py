@@ -1,5 +1,5 @@
 """Far-field propagation by MFT, drop-in for ``lentil.propagate_dft``
-(lentil/propagate.py:345-470).
+(lentil/propagate.py:147-272).
 
 The window algebra (tilt -> integer + subpixel shift, output/mask window
 intersection, lentil's centring of the clipped window) runs on the host in
@@ -15,13 +15,13 @@ from .ptype import pupil, image
 
 
 def _dft_alpha(dx, du, wavelength, z, oversample):
-    """lentil/propagate.py:319-321."""
+    """lentil/propagate.py:121-123."""
     return ((dx[0] * du[0]) / (wavelength * z * oversample),
             (dx[1] * du[1]) / (wavelength * z * oversample))
 
 
 def _propagate_ptype(ptype, method='fraunhofer'):
-    """lentil/propagate.py:461-470."""
+    """lentil/propagate.py:263-272."""
     if ptype not in (pupil, image):
         raise TypeError("Wavefront must have ptype 'pupil' or 'image'")
     return image if ptype == pupil else pupil
@@ -29,7 +29,7 @@ def _propagate_ptype(ptype, method='fraunhofer'):
 
 def _mask_window(mask):
     """Shape and centre shift of the nonzero region of an output mask
-    (lentil/propagate.py:443-458)."""
+    (lentil/propagate.py:245-260)."""
     rmin, rmax, cmin, cmax = util.boundary(mask, 0)
     shape = (rmax - rmin + 1, cmax - cmin + 1)
     shift = (rmin + shape[0] // 2 - mask.shape[0] // 2, cmin + shape[1] // 2 - mask.shape[1] // 2)
@@ -46,7 +46,7 @@ class FieldJob:
 
 
 def plan_fields(wavefront, pixelscale, shape=None, prop_shape=None, oversample=2, mask=None):
-    """Window maths of propagate_dft for every field (lentil/propagate.py:373-438).
+    """Window maths of propagate_dft for every field (lentil/propagate.py:175-240).
 
     Returns (ptype_out, shape_out, du, jobs); a field whose window misses the
     output produces no job, as in lentil."""
@@ -78,7 +78,7 @@ def plan_fields(wavefront, pixelscale, shape=None, prop_shape=None, oversample=2
         ishape = ext.intersection_shape(out_extent, prop_extent)
         ishift = ext.intersection_shift(out_extent, prop_extent)
         iextent = ext.array_extent(ishape, ishift)
-        # extra shift that re-centres a clipped window (lentil/propagate.py:419-428)
+        # extra shift that re-centres a clipped window (lentil/propagate.py:221-230)
         pshift = np.array(ext.array_center(prop_extent)) - np.array(ext.array_center(iextent))
         alpha = _dft_alpha(dx, du, wavefront.wavelength, z, oversample)
         jobs.append(FieldJob(field, alpha, ishape, pshift + subpx, ishift))
@@ -88,7 +88,7 @@ def plan_fields(wavefront, pixelscale, shape=None, prop_shape=None, oversample=2
 def propagate_dft(wavefront, pixelscale, shape=None, prop_shape=None, oversample=2, mask=None,
                   precision='fp64'):
     """Propagate a Wavefront to the far field with the MFT
-    (lentil/propagate.py:345-440).  ``precision`` selects the complex128
+    (lentil/propagate.py:147-242).  ``precision`` selects the complex128
     path (default, lentil parity) or the split tensor-core path."""
     from .wavefront import Wavefront
     ptype_out, shape_out, du, jobs = plan_fields(wavefront, pixelscale, shape, prop_shape,
