@@ -482,6 +482,22 @@ def run_monochromatic(args):
     cpu_s = time.perf_counter() - t0
     e_api = lo.peak_normalised_error(api().cpu().numpy(), ref)
     e_fused = lo.peak_normalised_error(plan.execute(A, O, W).cpu().numpy()[0], ref)
+    # propagate_fft on the same pupil (666^2 centred FFT, cropped to 256^2):
+    # the drop-in API in complex128 and split precision vs numpy's FFT
+    fft_legs = {}
+    t0 = time.perf_counter()
+    ref_fft = lo.propagate_fft(lo.Wavefront(650e-9) * ref_pl, wl.det_pixelscale, shape=wl.det_shape,
+                               oversample=wl.oversample).intensity
+    cpu_fft_s = time.perf_counter() - t0
+    for prec in ('fp64', 'split-bf16'):
+        call = lambda: lg.propagate_fft(lg.Wavefront(650e-9) * pl, wl.det_pixelscale,
+                                        shape=wl.det_shape, oversample=wl.oversample,
+                                        precision=prec).intensity_tensor()
+        m_, p50_, p99_ = _timed(call, args.steps, args.warmup)
+        fft_legs[prec] = {'value': 1e3 / m_, 'unit': 'PSFs/s', 'p50_ms': p50_, 'p99_ms': p99_,
+                          'err_vs_oracle': lo.peak_normalised_error(call().cpu().numpy(), ref_fft)}
+    fft_legs['cpu_baseline'] = {'value': 1.0 / cpu_fft_s, 'unit': 'PSFs/s', 'cores': os.cpu_count(),
+                                'kind': 'port', 'sample': 'one PSF through the numpy FFT restatement'}
     line = {'metric': 'monochromatic 256^2 PSFs/s', 'value': 1e3 / f_mean, 'unit': 'PSFs/s',
             'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': f_mean,
             'p50_ms': f_p50, 'p99_ms': f_p99, 'higher_is_better': True,
@@ -491,6 +507,7 @@ def run_monochromatic(args):
             'api_fp64': {'value': 1e3 / api_mean, 'p50_ms': api_p50, 'p99_ms': api_p99,
                          'err_vs_oracle': e_api},
             'err_vs_oracle': e_fused,
+            'propagate_fft': fft_legs,
             'cpu_baseline': {'value': 1.0 / cpu_s, 'unit': 'PSFs/s', 'cores': os.cpu_count(),
                              'kind': 'port', 'sample': 'one PSF through the oracle'}}
     print(json.dumps(line), flush=True)

@@ -160,6 +160,46 @@ int lgb_pixelate(const double* img, int rows, int cols, int oversample, double* 
                  void* workspace, size_t workspace_bytes, lgb_stream stream);
 
 /* ------------------------------------------------------------------------
+ * Plane.fit_tilt (lentil/plane.py:522-611) without forming ptt_vector.
+ * opd: [H][W]; mask: [S][H][W] (S masks; S = 1 for a 2-D mask), float64.
+ * lgb_ptt_normal writes, per mask s, the normal equations of lentil's
+ * least-squares fit in the basis b = [1, r*ps_r, -c*ps_c] (r, c centred
+ * mesh, lentil/helper.py:7-17):
+ *   out[9s .. 9s+8] = {A00 A01 A02 A11 A12 A22 y0 y1 y2},
+ *   A = sum m^2 b b^T, y = sum m b opd  (deterministic FP64 sums);
+ * workspace: lgb_ptt_normal_workspace_size(S) bytes.
+ * lgb_remove_tilt, given t[3s..3s+2] = (piston, x, y) of every mask, writes
+ * lentil's tilt-free OPD: S == 1: opd - m (t1 r ps_r - t2 c ps_c);
+ * S > 1: sum_s (opd - m_s (t_s1 r ps_r - t_s2 c ps_c)) m_s.
+ * ---------------------------------------------------------------------- */
+size_t lgb_ptt_normal_workspace_size(int S);
+int lgb_ptt_normal(const double* opd, const double* mask, int S, int H, int W, double ps_r,
+                   double ps_c, double* out, void* workspace, size_t workspace_bytes,
+                   lgb_stream stream);
+int lgb_remove_tilt(const double* opd, const double* mask, int S, int H, int W, double ps_r,
+                    double ps_c, const double* t, double* out, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Zernike generators (lentil/zernike.py:11-234, 444-480).  mask: [H][W]
+ * float64, nonzero = inside.
+ * lgb_zernike_coordinates: rho, theta of lentil's zernike_coordinates; the
+ * origin is the mask centroid when auto_shift != 0 (one 24-byte read back
+ * to the host), else (shift_r, shift_c) pixels from the centre; rotate in
+ * degrees.  workspace: lgb_zernike_workspace_size() bytes.
+ * lgb_zernike_eval: table (device, K rows of 3 + 2T doubles) =
+ *   [m, scale, nterms, (coef, power) x T]; out = sum_j scale_j R_j(rho)
+ *   ang_j(theta) mask (basis == 0, [H][W]) or every term ([K][H][W]);
+ *   ang = cos(m theta) for m > 0, sin(m theta) for m < 0, 1 for m == 0.
+ * ---------------------------------------------------------------------- */
+size_t lgb_zernike_workspace_size(void);
+int lgb_zernike_coordinates(const double* mask, int H, int W, int auto_shift, double shift_r,
+                            double shift_c, double rotate, double* rho, double* theta,
+                            void* workspace, size_t workspace_bytes, lgb_stream stream);
+int lgb_zernike_eval(const double* rho, const double* theta, const double* mask, size_t count,
+                     const double* table, int K, int T, double* out, int basis,
+                     lgb_stream stream);
+
+/* ------------------------------------------------------------------------
  * Gradient building blocks (no counterpart in lentil, which has no
  * gradients; they make the MFT path differentiable for phase retrieval).
  * For I = |F|^2 with F = dft2(f), f = amp exp(2 pi i opd / lambda):

@@ -1,7 +1,7 @@
 """lentil_gb300: lentil's far-field MFT diffraction path on one GB300 (sm_103a).
 
 Drop-in API of the path (same names and arguments as lentil 0.8.8):
-``fourier.dft2``/``idft2``, ``propagate_dft``, ``Wavefront``, ``Plane``,
+``fourier.dft2``/``idft2``, ``propagate_dft``, ``propagate_fft``, ``Wavefront``, ``Plane``,
 ``Pupil``, ``Image``, ``Tilt``, ``field`` helpers and ``detector.pixelate``,
 plus the fused ``broadband_psf``/``PSFPlan``.  Every transform, phasor,
 overlap-add and pixelation runs in the library's own CUDA kernels
@@ -18,7 +18,7 @@ from . import field
 from .field import Field
 from .plane import Plane, Pupil, Image, Tilt
 from .wavefront import Wavefront
-from .propagate import propagate_dft
+from .propagate import propagate_dft, propagate_fft, scratch_shape
 from .broadband import broadband_psf, PSFPlan
 from .shapes import circle, hexagon, rectangle, spider, hex_segments
 from .util import boundary, centroid, normalize_power, pad

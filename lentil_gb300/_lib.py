@@ -57,6 +57,17 @@ SIGNATURES = {
     'lgb_pixel': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
     'lgb_pixelate': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t,
                              c_void_p]),
+    'lgb_ptt_normal_workspace_size': (c_size_t, [c_int]),
+    'lgb_ptt_normal': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_double, c_double,
+                               c_void_p, c_void_p, c_size_t, c_void_p]),
+    'lgb_remove_tilt': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_double, c_double,
+                                c_void_p, c_void_p, c_void_p]),
+    'lgb_zernike_workspace_size': (c_size_t, []),
+    'lgb_zernike_coordinates': (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_double,
+                                        c_double, c_void_p, c_void_p, c_void_p, c_size_t,
+                                        c_void_p]),
+    'lgb_zernike_eval': (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_int, c_int,
+                                 c_void_p, c_int, c_void_p]),
     'lgb_abs2': (c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
     'lgb_intensity_adjoint': (c_int, [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     'lgb_phasor_adjoint': (c_int, [c_void_p, c_void_p, c_int, c_int, c_double, c_void_p, c_int,

@@ -270,27 +270,44 @@ class Plane(_PlaneBase):
         return v
 
     def fit_tilt(self, inplace=False):
-        """Least-squares tilt removal into Tilt objects (lentil/plane.py:564-611)."""
+        """Least-squares tilt removal into Tilt objects (lentil/plane.py:564-611).
+
+        The fit runs on the GPU without forming ``ptt_vector``: one kernel
+        sums each mask's 3x3 normal equations of lentil's least-squares
+        problem (deterministic FP64), the host solves them with ``lstsq``
+        (the minimum-norm solution lentil's ``lstsq`` returns), and a second
+        kernel removes the tilts with lentil's one-mask / several-mask rules.
+        The OPD keeps its kind (numpy stays numpy, a CUDA tensor stays one)."""
         plane = self if inplace else copy.deepcopy(self)
-        v = plane.ptt_vector()
-        opd = _np(plane.opd).astype(float)
-        if v is None or opd.size == 1:
+        if plane.shape == () or plane.shape is None:
+            return plane                       # no mask: ptt_vector is None
+        if plane.pixelscale is None:
+            raise ValueError("can't create ptt_vector with pixelscale = ()")
+        opd_in = plane.opd
+        if _size(opd_in) == 1:
             return plane
-        mask = _np(self.mask)
-        if self.size == 1:
-            t = np.linalg.lstsq(v.T, opd.ravel(), rcond=None)[0]
-            opd = opd - np.einsum('ij,i->j', v[1:3], t[1:3]).reshape(opd.shape)
-            plane.opd = opd
-            plane.tilt.append(Tilt(x=t[1], y=t[2]))
-        else:
-            t = np.empty((self.size, 3))
-            acc = np.zeros_like(opd)
-            for k in range(self.size):
-                t[k] = np.linalg.lstsq(v[3 * k:3 * k + 3].T, opd.ravel(), rcond=None)[0]
-                seg = np.einsum('ij,i->j', v[3 * k + 1:3 * k + 3], t[k, 1:3])
-                acc += (opd - seg.reshape(opd.shape)) * mask[k]
-            plane.opd = acc
-            plane.tilt.extend([Tilt(x=t[k, 1], y=t[k, 2]) for k in range(self.size)])
+        H, W = (int(x) for x in plane.shape)
+        S = plane.size
+        ps = np.broadcast_to(plane.pixelscale, (2,)).astype(float)
+        dev = dv.device()
+        opd_d = dv.to_device(opd_in, torch.float64).reshape(H, W).contiguous()
+        mask_d = dv.to_device(plane.mask, torch.float64).reshape(S, H, W).contiguous()
+        sums = torch.empty((S, 9), dtype=torch.float64, device=dev)
+        ws = dv.workspace(_lib.load().lgb_ptt_normal_workspace_size(S))
+        _lib.call('lgb_ptt_normal', opd_d.data_ptr(), mask_d.data_ptr(), S, H, W, float(ps[0]),
+                  float(ps[1]), sums.data_ptr(), ws.data_ptr(), ws.numel(), dv.stream_ptr())
+        q = dv.to_host(sums)
+        t = np.empty((S, 3))
+        for k in range(S):
+            a00, a01, a02, a11, a12, a22, y0, y1, y2 = q[k]
+            A = np.array([[a00, a01, a02], [a01, a11, a12], [a02, a12, a22]])
+            t[k] = np.linalg.lstsq(A, np.array([y0, y1, y2]), rcond=None)[0]
+        t_d = torch.as_tensor(t, device=dev).contiguous()
+        out = torch.empty((H, W), dtype=torch.float64, device=dev)
+        _lib.call('lgb_remove_tilt', opd_d.data_ptr(), mask_d.data_ptr(), S, H, W, float(ps[0]),
+                  float(ps[1]), t_d.data_ptr(), out.data_ptr(), dv.stream_ptr())
+        plane.opd = out if dv.is_tensor(opd_in) else dv.to_host(out)
+        plane.tilt.extend([Tilt(x=t[k, 1], y=t[k, 2]) for k in range(S)])
         return plane
 
 

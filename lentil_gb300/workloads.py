@@ -16,7 +16,7 @@ import numpy as np
 
 from . import shapes, util
 from .wfe import blackbody_photlam
-from .zernike import zernike as zernike_mode, zernike_coordinates
+from .zernike import zernike_basis, zernike_compose, zernike_coordinates
 
 
 class Workload:
@@ -60,15 +60,11 @@ def broadband_segmented(npix=1024, n_wavelengths=64, seed=2, seg_radius=None):
     gmask = segs.sum(axis=0)
     amp = util.normalize_power(gmask)
     basis, sigma = [], []
-    for s in segs:
-        rho, theta = zernike_coordinates(s)
-        for j in (1, 2, 3):                       # piston, tip, tilt of this segment
-            basis.append(zernike_mode(s, j, rho=rho, theta=theta).astype(np.float32))
-            sigma.append(50e-9)
-    rho, theta = zernike_coordinates(gmask)
-    for j in range(2, 23):                        # global Noll 2-22
-        basis.append(zernike_mode(gmask, j, rho=rho, theta=theta).astype(np.float32))
-        sigma.append(15e-9)
+    for s in segs:                                # piston, tip, tilt of each segment
+        basis.extend(zernike_basis(s, [1, 2, 3]).astype(np.float32))
+        sigma.extend([50e-9] * 3)
+    basis.extend(zernike_basis(gmask, range(2, 23)).astype(np.float32))   # global Noll 2-22
+    sigma.extend([15e-9] * 21)
     wl_nm = np.linspace(500.0, 900.0, n_wavelengths)
     w = blackbody_photlam(wl_nm, 5800.0)
     return Workload('broadband_segmented', amp, segs, np.asarray(basis), np.asarray(sigma),
@@ -79,9 +75,7 @@ def monochromatic_circle(seed=1):
     """The monochromatic circular-pupil workload (see module docstring)."""
     npix = 256
     amp = util.normalize_power(shapes.circle((npix, npix), npix // 2, antialias=False))
-    rho, theta = zernike_coordinates(amp)
-    basis = np.asarray([zernike_mode(amp, j, rho=rho, theta=theta).astype(np.float32)
-                        for j in range(2, 12)])
+    basis = zernike_basis(amp, range(2, 12)).astype(np.float32)
     return Workload('monochromatic_circle', amp, None, basis, np.full(10, 20e-9),
                     np.array([650e-9]), np.array([1.0]), 1.0 / npix, 10.0, 5e-6, 128, 2, seed)
 
@@ -106,17 +100,14 @@ def large_segmented(npix=4096, n_wavelengths=32, seed=5, tilt_lambda_d=50.0):
     rng = np.random.default_rng(seed)
     support = mask > 0
     rho, theta = zernike_coordinates(support)
-    opd = np.zeros((npix, npix))
-    for j, c in zip(range(2, 23), rng.normal(0, 15e-9, 21)):
-        opd += c * zernike_mode(support, j, rho=rho, theta=theta)
+    opd = zernike_compose(support, np.r_[0.0, rng.normal(0, 15e-9, 21)], rho=rho, theta=theta)
     from .wfe import power_spectrum
     opd += power_spectrum(support, 1.0 / npix, 25e-9, 10.0, 2, seed=seed)
     # tilt of tilt_lambda_d lambda/D at 800 nm in a random direction: Noll
     # Z2/Z3 = 2 rho cos/sin, so a coefficient c gives 4c of OPD across D
     ang = rng.uniform(0, 2 * np.pi)
     c = tilt_lambda_d * 800e-9 / 4
-    opd += c * np.cos(ang) * zernike_mode(support, 2, rho=rho, theta=theta)
-    opd += c * np.sin(ang) * zernike_mode(support, 3, rho=rho, theta=theta)
+    opd += zernike_compose(support, [0.0, c * np.cos(ang), c * np.sin(ang)], rho=rho, theta=theta)
     wl_nm = np.linspace(600.0, 1000.0, n_wavelengths)
     w = blackbody_photlam(wl_nm, 5800.0)
     wl = Workload('large_segmented', amp, None, np.zeros((0, npix, npix), np.float32),

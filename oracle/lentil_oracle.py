@@ -14,6 +14,7 @@ from __future__ import annotations
 import copy
 import functools
 import itertools
+from math import factorial
 
 import numpy as np
 
@@ -681,6 +682,70 @@ def propagate_dft(wavefront, pixelscale, shape=None, prop_shape=None, oversample
     return out
 
 
+def _fft_shape(dx, du, z, wavelength, oversample):
+    """Padded FFT shape and the propagation wavelength it implies;
+    lentil/propagate.py:126-132 (``_dft_alpha`` is symmetric in wavelength
+    and z, so lentil's swapped argument order is harmless)."""
+    alpha = _dft_alpha(dx, du, z, wavelength, oversample)
+    fft_shape = np.round(np.reciprocal(alpha)).astype(int)
+    prop_wavelength = np.min((fft_shape / oversample * dx * du) / z)
+    return fft_shape, prop_wavelength
+
+
+def _fft2c(x):
+    """Centred ortho FFT; lentil/propagate.py:135-136."""
+    return np.fft.ifftshift(np.fft.fft2(np.fft.fftshift(x), norm='ortho'))
+
+
+def _has_tilt(wavefront):
+    """lentil/propagate.py:139-144."""
+    return any(f.tilt for f in wavefront.data)
+
+
+def scratch_shape(wavelength, dx, du, z, oversample):
+    """lentil/propagate.py:91-118."""
+    dx = np.broadcast_to(dx, (2,))
+    du = np.broadcast_to(du, (2,))
+    fft_shape, _ = _fft_shape(dx, du, z, np.max(wavelength), oversample)
+    return tuple(fft_shape)
+
+
+def propagate_fft(wavefront, pixelscale, shape=None, oversample=2, scratch=None):
+    """Far-field propagation by a zero-padded centred FFT;
+    lentil/propagate.py:9-88."""
+    if _has_tilt(wavefront):
+        raise NotImplementedError('propagate_fft does not support Wavefronts with fitted tilt. '
+                                  'Use propagate_dft instead.')
+    ptype_out = _propagate_ptype(wavefront.ptype)
+    pixelscale = np.broadcast_to(pixelscale, (2,))
+    fft_shape, prop_wavelength = _fft_shape(wavefront.pixelscale, pixelscale,
+                                            wavefront.focal_length, wavefront.wavelength,
+                                            oversample)
+    if shape is None:
+        shape_out = tuple(fft_shape)
+    else:
+        shape = tuple(np.broadcast_to(shape, (2,)))
+        if np.any(shape > fft_shape / oversample):
+            raise ValueError(f'requested shape {tuple(shape)} is larger in at least one '
+                             f'dimension than maximum propagation shape '
+                             f'{tuple(fft_shape // oversample)}')
+        shape_out = (shape[0] * oversample, shape[1] * oversample)
+    out = Wavefront.empty(wavelength=prop_wavelength, pixelscale=pixelscale / oversample,
+                          focal_length=wavefront.focal_length, shape=shape_out, ptype=ptype_out)
+    if scratch is not None:
+        if not all(np.asarray(scratch.shape) > fft_shape):
+            raise ValueError(f'scratch must have shape greater than or equal to {tuple(fft_shape)}')
+        view = scratch[0:fft_shape[0], 0:fft_shape[1]]
+        view[...] = 0
+        for f in wavefront.data:
+            view[...] = insert(f, view)
+        field = _fft2c(view)
+    else:
+        field = _fft2c(pad(wavefront.field, fft_shape))
+    out.data.append(Field(data=field, pixelscale=pixelscale / oversample))
+    return out
+
+
 def broadband_psf(pupil, wavelengths, weights, pixelscale, shape=None, prop_shape=None,
                   oversample=2, mask=None, out=None):
     """The documented user broadband loop (docs/user/performance.rst:44-49):
@@ -709,6 +774,130 @@ def pixel(img, oversample=1):
 def pixelate(img, oversample):
     """lentil/detector.py:225-251."""
     return rescale(pixel(img, oversample), 1 / oversample, order=3, mode='nearest', unitary=True)
+
+
+# --------------------------------------------------------------------------
+# input generators (lentil/zernike.py, lentil/wfe.py)
+# --------------------------------------------------------------------------
+def noll_to_nm(j):
+    """lentil/zernike.py:348-391 (row of the triangle, then the position in it)."""
+    if j < 1:
+        raise ValueError('Noll index must be greater than zero')
+    n = int(np.ceil((-1 + np.sqrt(1 + 8 * j)) / 2) - 1)
+    if n == 0:
+        return 0, 0
+    r = int(j - (n + 1) * (n + 2) / 2 - 1)
+    row = [1, 1] if n & 1 else [0]
+    for _ in range(n // 2):
+        row.append(row[-1] + 2)
+        row.append(row[-1])
+    return int(n), int(row[r] * (-1 if j & 1 else 1))
+
+
+def ansi_to_nm(j):
+    """lentil/zernike.py:394-415."""
+    if j < 0:
+        raise ValueError('ANSI index must be zero or larger')
+    n = np.floor((np.sqrt(8 * j + 1) - 1) / 2)
+    return int(n), int(2 * j - n * (n + 2))
+
+
+def fringe_to_nm(j):
+    """lentil/zernike.py:418-441."""
+    if j < 1:
+        raise ValueError('Fringe index must be greater than zero')
+    m_n = 2 * (np.ceil(np.sqrt(j)) - 1)
+    g_s = (m_n / 2) ** 2 + 1
+    n = m_n / 2 + np.floor((j - g_s) / 2)
+    return int(n), int((m_n - n) * (1 - np.mod(j - g_s, 2) * 2))
+
+
+def zernike_radial(n, m, rho):
+    """lentil/zernike.py:96-109."""
+    m, n = abs(int(m)), abs(int(n))
+    if (n - m) & 1:
+        return 0
+    out = np.zeros(rho.shape)
+    for k in range((n - m) // 2 + 1):
+        rk = ((-1) ** k * factorial(n - k) /
+              (factorial(k) * factorial((n + m) // 2 - k) * factorial((n - m) // 2 - k)))
+        out += rk * rho ** (n - 2 * k)
+    return out
+
+
+def zernike_coordinates(mask, shift=None, rotate=0):
+    """lentil/zernike.py:444-480."""
+    mask = np.asarray(mask, dtype=bool)
+    if shift is None:
+        center = np.asarray(mask.shape) / 2
+        cen = centroid(mask)
+        shift = (cen[0] - center[0], cen[1] - center[1])
+    rr, cc = mesh(mask.shape, shift)
+    r = np.abs(rr + 1j * cc)
+    rho = r / np.max(r * mask)
+    angle = (90 - rotate) * np.pi / 180
+    theta = np.angle(-rr * np.exp(1j * angle) + 1j * cc * np.exp(1j * angle))
+    return rho, theta
+
+
+def zernike(mask, index, normalize=True, order='noll', rho=None, theta=None):
+    """lentil/zernike.py:11-93."""
+    mask = np.asarray(mask, dtype=bool)
+    n, m = {'noll': noll_to_nm, 'fringe': fringe_to_nm, 'ansi': ansi_to_nm}[order](index)
+    if rho is None:
+        rho, theta = zernike_coordinates(mask)
+    elif theta is None:
+        raise ValueError('Both rho and theta must be specified')
+    if m == 0:
+        if n == 0:
+            return mask
+        return (np.sqrt(n + 1) if normalize else 1) * zernike_radial(n, m, rho) * mask
+    ang = np.cos(m * theta) if m > 0 else np.sin(m * theta)
+    if normalize:
+        return np.sqrt(2) * np.sqrt(n + 1) * zernike_radial(n, m, rho) * ang * mask
+    return zernike_radial(n, m, rho) * ang * mask
+
+
+def zernike_compose(mask, coeffs, normalize=True, order='noll', rho=None, theta=None):
+    """lentil/zernike.py:112-180."""
+    mask = np.asarray(mask)
+    opd = np.zeros(mask.shape)
+    for index, coeff in np.ndenumerate(np.asarray(coeffs)):
+        opd += coeff * zernike(mask, index[0] + 1, normalize, order, rho, theta)
+    return opd
+
+
+def zernike_basis(mask, modes, vectorize=False, normalize=True, order='noll', rho=None,
+                  theta=None):
+    """lentil/zernike.py:183-234."""
+    modes = np.asarray(modes)
+    if modes.shape == ():
+        modes = modes[..., np.newaxis]
+    mask = np.asarray(mask)
+    basis = np.zeros(modes.shape + mask.shape)
+    for index, mode in np.ndenumerate(modes):
+        basis[index] = zernike(mask, mode, normalize, order, rho, theta)
+    return basis.reshape(basis.shape[0], -1) if vectorize else basis
+
+
+def power_spectrum(mask, pixelscale, rms, half_power_freq, exp, seed=None):
+    """lentil/wfe.py:8-70 (Sidick 2009 PSD filter of seeded white noise)."""
+    mask = np.asarray(mask)
+    rng = np.random.default_rng(seed)
+    n, m = mask.shape
+    yy, xx = np.mgrid[0:m, 0:n]
+    yy = (yy - (np.floor(m / 2) + 1)) / m
+    xx = (xx - (np.floor(n / 2) + 1)) / n
+    dr = np.sqrt(xx * xx + yy * yy)
+    half_power_freq = half_power_freq * pixelscale / np.sqrt(m ** 2 + n ** 2)
+    psd = 1 / (1 + (dr / half_power_freq) ** exp)
+    psd[dr == 0] = 0
+    psd = psd / np.sum(psd)
+    H = np.fft.fftshift(np.sqrt(psd))
+    noise = rng.normal(size=[n, m])
+    opd = np.real(np.fft.ifft2(np.fft.fft2(noise) * H)) * np.sqrt(m * n)
+    opd *= mask
+    return opd * np.sqrt(np.count_nonzero(opd) / np.sum(np.abs(opd) ** 2)) * rms
 
 
 # --------------------------------------------------------------------------

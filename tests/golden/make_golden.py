@@ -24,6 +24,7 @@ def main(ref_root):
     import lentil.field
     import lentil.fourier
     import lentil.helper
+    import lentil.propagate
     import lentil.radiometry
 
     rng = np.random.default_rng(20261203)
@@ -220,6 +221,66 @@ def main(ref_root):
     bb = lentil.radiometry.Blackbody(wl, 5800).value
     g['bb_wl_nm'], g['bb_value'] = wl, bb
     np.savez_compressed(os.path.join(HERE, 'generators.npz'), **g)
+
+    # ------------------------------------------------------- propagate_fft
+    # own generator so that the fixtures above do not change
+    rf = np.random.default_rng(20261204)
+    q = {}
+
+    def fft_case(name, pl, wl, keep=48, **kw):
+        w = lentil.propagate_fft(lentil.Wavefront(wl) * pl, **kw)
+        field = w.data[0].data
+        q[f'{name}_amp'] = np.asarray(pl.amplitude, float)
+        q[f'{name}_opd'] = np.array(np.broadcast_to(np.asarray(pl.opd, float), pl.amplitude.shape))
+        q[f'{name}_pixelscale_in'] = np.asarray(pl.pixelscale, float)
+        q[f'{name}_focal_length'] = np.asarray(pl.focal_length, float)
+        q[f'{name}_wavelength'] = np.asarray(wl, float)
+        q[f'{name}_pixelscale'] = np.asarray(kw['pixelscale'], float)
+        q[f'{name}_shape'] = np.asarray(-1 if kw.get('shape') is None else kw['shape'])
+        q[f'{name}_oversample'] = np.asarray(kw.get('oversample', 2))
+        q[f'{name}_scratch'] = np.asarray(-1 if kw.get('scratch') is None else kw['scratch'].shape)
+        q[f'{name}_intensity'] = w.intensity
+        q[f'{name}_out_shape'] = np.asarray(w.shape)
+        q[f'{name}_out_wavelength'] = np.asarray(w.wavelength, float)
+        q[f'{name}_out_pixelscale'] = np.asarray(w.pixelscale, float)
+        q[f'{name}_field_shape'] = np.asarray(field.shape)
+        # centre crop of the full FFT field (the whole array is large)
+        k = min(keep, *field.shape)
+        r0, c0 = (field.shape[0] - k) // 2, (field.shape[1] - k) // 2
+        q[f'{name}_field_crop'] = field[r0:r0 + k, c0:c0 + k]
+        q[f'{name}_field_crop_origin'] = np.asarray([r0, c0])
+        if kw.get('scratch') is not None:     # lentil leaves the padded field in scratch
+            reg = kw['scratch'][:field.shape[0], :field.shape[1]]
+            q[f'{name}_scratch_sum'] = np.asarray(reg.sum())
+            q[f'{name}_scratch_crop'] = reg[r0:r0 + k, c0:c0 + k]
+
+    # the monochromatic workload pupil: fft shape 666 (even), cropped to 256^2
+    c = np.concatenate([[0.0], rf.normal(0, 20e-9, 10)])
+    amp = lentil.normalize_power(lentil.circle((256, 256), 128, antialias=False))
+    pl = lentil.Pupil(amplitude=amp, opd=lentil.zernike_compose(amp, c), pixelscale=1 / 256,
+                      focal_length=10)
+    fft_case('c1', pl, 650e-9, pixelscale=5e-6, shape=128, oversample=2)
+    # odd pupil, per-axis pixelscale, odd fft shape (153 x 191), shape=None, oversample 1
+    amp = lentil.normalize_power(lentil.circle((127, 127), 60))
+    opd = lentil.zernike_compose(amp, np.concatenate([[0.0], rf.normal(0, 40e-9, 8)]))
+    pl = lentil.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 127, focal_length=10)
+    lam = (1 / 127) * 5e-6 * 153 / 10
+    fft_case('odd', pl, lam, pixelscale=(5e-6, 4e-6), oversample=1)
+    # the same through a scratch array (lentil centres by field.insert there)
+    scratch = np.full((160, 200), 7 + 0j)
+    fft_case('odd_scratch', pl, lam, pixelscale=(5e-6, 4e-6), oversample=1, scratch=scratch)
+    # field larger than the fft shape: lentil's pad crops it (fft 151 x 151)
+    amp = lentil.normalize_power(lentil.circle((200, 200), 98))
+    opd = lentil.zernike_compose(amp, np.concatenate([[0.0], rf.normal(0, 30e-9, 6)]))
+    pl = lentil.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 200, focal_length=10)
+    fft_case('crop', pl, (1 / 200) * 5e-6 * 151 / 10, pixelscale=5e-6, shape=(60, 70),
+             oversample=1)
+    # scratch_shape over a wavelength list
+    q['scratch_shape_args'] = np.asarray([1 / 256, 5e-6, 10, 2])
+    q['scratch_shape_wl'] = np.asarray([500e-9, 650e-9, 900e-9])
+    q['scratch_shape'] = np.asarray(lentil.scratch_shape([500e-9, 650e-9, 900e-9], 1 / 256,
+                                                         5e-6, 10, 2))
+    np.savez_compressed(os.path.join(HERE, 'propagate_fft.npz'), **q)
     print('golden fixtures written to', HERE)
 
 

@@ -3,7 +3,8 @@ import numpy as np
 import pytest
 
 from oracle import lentil_oracle as lo
-from tests.golden_cases import PROPAGATE_CASES, build_pupil, propagate_kwargs
+from tests.golden_cases import (FFT_CASES, PROPAGATE_CASES, build_pupil, fft_case, fft_field_crop,
+                                propagate_kwargs)
 
 
 def test_dft2_cases(golden):
@@ -89,3 +90,27 @@ def test_pixelate(golden, name):
     img, os_ = g[f'{name}_img'], int(g[f'{name}_os'])
     assert lo.peak_normalised_error(lo.pixel(img, os_), g[f'{name}_pixel']) < 1e-13
     assert lo.peak_normalised_error(lo.pixelate(img, os_), g[f'{name}_pixelate']) < 1e-12
+
+
+@pytest.mark.parametrize('name', FFT_CASES)
+def test_propagate_fft_cases(golden, name):
+    g = golden('propagate_fft')
+    wf, kw, scratch = fft_case(lo, g, name)
+    w = lo.propagate_fft(wf, scratch=scratch, **kw)
+    assert tuple(w.shape) == tuple(g[f'{name}_out_shape'])
+    assert w.wavelength == float(g[f'{name}_out_wavelength'])
+    assert np.array_equal(w.pixelscale, g[f'{name}_out_pixelscale'])
+    field = w.data[0].data
+    assert field.shape == tuple(g[f'{name}_field_shape'])
+    assert lo.peak_normalised_error(fft_field_crop(g, name, field), g[f'{name}_field_crop']) < 1e-12
+    assert lo.peak_normalised_error(w.intensity, g[f'{name}_intensity']) < 1e-12
+    if scratch is not None:                  # lentil leaves the padded field in scratch
+        reg = scratch[:field.shape[0], :field.shape[1]]
+        assert np.isclose(reg.sum(), complex(g[f'{name}_scratch_sum']), rtol=1e-12)
+        assert np.array_equal(fft_field_crop(g, name, reg), g[f'{name}_scratch_crop'])
+
+
+def test_scratch_shape(golden):
+    g = golden('propagate_fft')
+    dx, du, z, os_ = g['scratch_shape_args']
+    assert lo.scratch_shape(g['scratch_shape_wl'], dx, du, z, os_) == tuple(g['scratch_shape'])
