@@ -180,6 +180,19 @@ int lgb_remove_tilt(const double* opd, const double* mask, int S, int H, int W, 
                     double ps_c, const double* t, double* out, lgb_stream stream);
 
 /* ------------------------------------------------------------------------
+ * power_spectrum (lentil/wfe.py:8-70): white noise (N x N, the caller's
+ * seeded normals) filtered by the Sidick PSD 1 / (1 + (f/f0)^exponent),
+ * times sqrt(N*N) and the mask, rescaled to `rms` over its nonzero pixels.
+ * lentil's grid makes this defined for square planes only.  N a power of
+ * two (<= 8192): FP64 radix-2 FFTs; other N: FP64 DFT matrices.
+ * workspace: lgb_power_spectrum_workspace_size(N) bytes.
+ * ---------------------------------------------------------------------- */
+size_t lgb_power_spectrum_workspace_size(int N);
+int lgb_power_spectrum(const double* noise, const double* mask, int N, double pixelscale,
+                       double rms, double half_power_freq, double exponent, double* out,
+                       void* workspace, size_t workspace_bytes, lgb_stream stream);
+
+/* ------------------------------------------------------------------------
  * Zernike generators (lentil/zernike.py:11-234, 444-480).  mask: [H][W]
  * float64, nonzero = inside.
  * lgb_zernike_coordinates: rho, theta of lentil's zernike_coordinates; the

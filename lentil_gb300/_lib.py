@@ -62,6 +62,9 @@ SIGNATURES = {
                                c_void_p, c_void_p, c_size_t, c_void_p]),
     'lgb_remove_tilt': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_double, c_double,
                                 c_void_p, c_void_p, c_void_p]),
+    'lgb_power_spectrum_workspace_size': (c_size_t, [c_int]),
+    'lgb_power_spectrum': (c_int, [c_void_p, c_void_p, c_int, c_double, c_double, c_double,
+                                   c_double, c_void_p, c_void_p, c_size_t, c_void_p]),
     'lgb_zernike_workspace_size': (c_size_t, []),
     'lgb_zernike_coordinates': (c_int, [c_void_p, c_int, c_int, c_int, c_double, c_double,
                                         c_double, c_void_p, c_void_p, c_void_p, c_size_t,

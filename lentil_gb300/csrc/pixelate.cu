@@ -11,6 +11,9 @@
 // when N is a multiple of os every sample falls on a grid point, so the
 // result is d = p[::os, ::os] rescaled by sum(p)/sum(d) and masked where
 // d == 0 -- the only case implemented.
+//
+// The same FFT machinery also filters white noise for lgb_power_spectrum
+// (lentil/wfe.py:8-70), defined at the end of this file.
 #include <algorithm>
 #include <cmath>
 
@@ -305,6 +308,128 @@ static int abs_reduce(int N, int os, const void* src, bool cplx, double* P, doub
   return LGB_OK;
 }
 
+// ------------------------------------------------------ power spectrum
+// psd(i, j) of lentil/wfe.py:41-52 on a square N x N grid: offsets from
+// (N//2 + 1), cycles per pixel, 1 / (1 + (dr/f0)^exp), 0 at dr == 0
+__device__ __forceinline__ double psd_at(int i, int j, int N, double f0, double expo) {
+  const double c = floor(N / 2.0) + 1.0;
+  const double yy = ((double)i - c) / N, xx = ((double)j - c) / N;
+  const double dr = sqrt(xx * xx + yy * yy);
+  return dr == 0.0 ? 0.0 : 1.0 / (1.0 + pow(dr / f0, expo));
+}
+
+constexpr int PSD_BLOCKS = 128;
+
+// fixed-order two-pass sums: pass 1 writes PSD_BLOCKS partials of (a, b)
+__device__ __forceinline__ void psd_block_store2(double a, double b, double* partial) {
+  __shared__ double sa[8], sb[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = a; sb[threadIdx.x >> 5] = b; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { ta += sa[w]; tb += sb[w]; }
+    partial[2 * blockIdx.x] = ta;
+    partial[2 * blockIdx.x + 1] = tb;
+  }
+}
+
+__global__ void __launch_bounds__(256) psd_sum_kernel(int N, double f0, double expo,
+                                                      double* __restrict__ partial) {
+  const size_t total = (size_t)N * N;
+  double a = 0.0;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < total;
+       p += (size_t)gridDim.x * blockDim.x)
+    a += psd_at((int)(p / N), (int)(p % N), N, f0, expo);
+  psd_block_store2(a, 0.0, partial);
+}
+
+// opd = Re(z) * N * mask (z complex or real), then (count of nonzero, sum opd^2)
+template <bool CPLX>
+__global__ void __launch_bounds__(256) psd_mask_kernel(const void* __restrict__ z,
+                                                       const double* __restrict__ mask, int N,
+                                                       double scale, double* __restrict__ opd,
+                                                       double* __restrict__ partial) {
+  const size_t total = (size_t)N * N;
+  double cnt = 0.0, ss = 0.0;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < total;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const double re = CPLX ? static_cast<const double2*>(z)[p].x : static_cast<const double*>(z)[p];
+    const double v = re * scale * mask[p];
+    opd[p] = v;
+    if (v != 0.0) { cnt += 1.0; ss += v * v; }
+  }
+  psd_block_store2(cnt, ss, partial);
+}
+
+__global__ void psd_final_kernel(const double* __restrict__ partial, int nblocks,
+                                 double* __restrict__ sums) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < nblocks; ++k) { a += partial[2 * k]; b += partial[2 * k + 1]; }
+    sums[0] = a;
+    sums[1] = b;
+  }
+}
+
+// Y *= fftshift(sqrt(psd / sum)); psd is symmetric under i <-> j, so the
+// transposed spectrum of the FFT path takes the same filter
+__global__ void psd_filter_kernel(double2* __restrict__ Y, int N, double f0, double expo,
+                                  const double* __restrict__ sums) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= N) return;
+  const int h = N / 2;                                  // fftshift: index k <- (k - N//2) mod N
+  const int si = (i - h + N) % N, sj = (j - h + N) % N;
+  const double H = sqrt(psd_at(si, sj, N, f0, expo) / sums[0]);
+  double2 v = Y[(size_t)i * N + j];
+  Y[(size_t)i * N + j] = make_double2(v.x * H, v.y * H);
+}
+
+__global__ void psd_rescale_kernel(double* __restrict__ opd, size_t count,
+                                   const double* __restrict__ sums, double rms) {
+  const double k = sqrt(sums[0] / sums[1]) * rms;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < count;
+       p += (size_t)gridDim.x * blockDim.x)
+    opd[p] *= k;
+}
+
+struct PsdSpace {
+  double* partial;
+  double* sums;          // [0] psd sum, then [0] count / [1] sum of squares
+  double2 *X, *Y, *tw;   // FFT path (tw only) / DFT path (E, Ec in tw's place)
+  double2 *E, *Ec;
+};
+
+static size_t psd_space(void* ws, int N, PsdSpace* s) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    off = align_up(off, 256);
+    void* p = ws ? static_cast<char*>(ws) + off : nullptr;
+    off += bytes;
+    return p;
+  };
+  PsdSpace t{};
+  const size_t NN = (size_t)N * N;
+  int logN;
+  t.partial = static_cast<double*>(take(2 * PSD_BLOCKS * sizeof(double)));
+  t.sums = static_cast<double*>(take(4 * sizeof(double)));
+  t.X = static_cast<double2*>(take(NN * sizeof(double2)));
+  t.Y = static_cast<double2*>(take(NN * sizeof(double2)));
+  if (fft_size(N, &logN)) {
+    t.tw = static_cast<double2*>(take((size_t)(N / 2) * sizeof(double2)));
+  } else {
+    t.E = static_cast<double2*>(take(NN * sizeof(double2)));
+    t.Ec = static_cast<double2*>(take(NN * sizeof(double2)));
+  }
+  if (s) *s = t;
+  return off;
+}
+
 }  // namespace lgb
 
 using namespace lgb;
@@ -350,6 +475,77 @@ extern "C" int lgb_pixelate(const double* img, int rows, int cols, int oversampl
   if (st) return st;
   if ((st = abs_reduce(N, os, src, cplx, nullptr, w.d, w.sums, s))) return st;
   pixelate_scale_kernel<<<cdiv(Nd * Nd, 256), 256, 0, s>>>(Nd * Nd, w.d, w.sums, out);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+extern "C" size_t lgb_power_spectrum_workspace_size(int N) {
+  if (N <= 0) return 0;
+  return psd_space(nullptr, N, nullptr);
+}
+
+extern "C" int lgb_power_spectrum(const double* noise, const double* mask, int N,
+                                  double pixelscale, double rms, double half_power_freq,
+                                  double exponent, double* out, void* workspace,
+                                  size_t workspace_bytes, lgb_stream stream) {
+  LGB_REQUIRE(noise && mask && out && workspace, LGB_EINVAL, "power_spectrum: null pointer");
+  LGB_REQUIRE(N > 0, LGB_EINVAL, "power_spectrum: size must be positive");
+  LGB_REQUIRE(workspace_bytes >= lgb_power_spectrum_workspace_size(N), LGB_EWORKSPACE,
+              "power_spectrum: workspace smaller than lgb_power_spectrum_workspace_size(N)");
+  cudaStream_t s = as_stream(stream);
+  PsdSpace w;
+  psd_space(workspace, N, &w);
+  const size_t NN = (size_t)N * N;
+  // half-power point in cycles per pixel (lentil/wfe.py:45): sqrt(m^2 + n^2)
+  const double f0 = half_power_freq * pixelscale / sqrt((double)N * N + (double)N * N);
+  const int blocks = std::max(1, std::min(4 * sm_count(), (int)((NN + 255) / 256)));
+  psd_sum_kernel<<<PSD_BLOCKS, 256, 0, s>>>(N, f0, exponent, w.partial);
+  psd_final_kernel<<<1, 32, 0, s>>>(w.partial, PSD_BLOCKS, w.sums);
+  real_to_complex_kernel<<<blocks, 256, 0, s>>>(noise, w.X, NN);
+  LGB_CUDA(cudaGetLastError());
+  int logN;
+  const double2* spatial;
+  if (fft_size(N, &logN)) {
+    const size_t smem = (size_t)N * sizeof(double2);
+    LGB_CUDA(cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  8192 * (int)sizeof(double2)));
+    const int threads = std::min(512, std::max(32, N / 2));
+    const dim3 tgrid(cdiv(N, 32), cdiv(N, 32)), tblock(32, 8);
+    twiddle_kernel<<<cdiv(std::max(N / 2, 1), 256), 256, 0, s>>>(N, w.tw);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w.X, N, logN, w.tw, 0);
+    transpose_c128_kernel<<<tgrid, tblock, 0, s>>>(w.X, w.Y, N);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w.Y, N, logN, w.tw, 0);          // Y = fft2(X)^T
+    psd_filter_kernel<<<dim3(cdiv(N, 128), N), 128, 0, s>>>(w.Y, N, f0, exponent, w.sums);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w.Y, N, logN, w.tw, 1);
+    transpose_c128_kernel<<<tgrid, tblock, 0, s>>>(w.Y, w.X, N);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w.X, N, logN, w.tw, 1);          // X = ifft2(...)
+    LGB_CUDA(cudaGetLastError());
+    spatial = w.X;
+  } else {
+    // DFT matrices E[u][r] = exp(-2 pi i u r / N) and their conjugate: the
+    // coordinate offset N//2 and shift -(N//2) undo the centring of the
+    // library's phase convention
+    PhaseAxis ax, axc;
+    int st;
+    if ((st = make_phase_axis(1.0 / N, -(double)(N / 2), (double)(N / 2), N, N, &ax))) return st;
+    if ((st = make_phase_axis(-1.0 / N, -(double)(N / 2), (double)(N / 2), N, N, &axc))) return st;
+    if ((st = launch_dft_matrix_c128(ax, N, N, w.E, true, s))) return st;
+    if ((st = launch_dft_matrix_c128(axc, N, N, w.Ec, true, s))) return st;
+    // fft2(X) = E X E (E symmetric); ifft2(Y) = Ec Y Ec / N^2
+    if ((st = launch_zgemm(N, N, N, w.E, N, 0, w.X, N, 0, w.Y, N, 0, 1, 1.0, s))) return st;
+    if ((st = launch_zgemm(N, N, N, w.Y, N, 0, w.E, N, 0, w.X, N, 0, 1, 1.0, s))) return st;
+    psd_filter_kernel<<<dim3(cdiv(N, 128), N), 128, 0, s>>>(w.X, N, f0, exponent, w.sums);
+    LGB_CUDA(cudaGetLastError());
+    const double inv = 1.0 / ((double)N * (double)N);
+    if ((st = launch_zgemm(N, N, N, w.Ec, N, 0, w.X, N, 0, w.Y, N, 0, 1, 1.0, s))) return st;
+    if ((st = launch_zgemm(N, N, N, w.Y, N, 0, w.Ec, N, 0, w.X, N, 0, 1, inv, s))) return st;
+    spatial = w.X;
+  }
+  // opd = Re(.) * sqrt(N * N) * mask, rescaled to rms over its nonzero pixels
+  psd_mask_kernel<true><<<PSD_BLOCKS, 256, 0, s>>>(spatial, mask, N, sqrt((double)N * N), out,
+                                                   w.partial);
+  psd_final_kernel<<<1, 32, 0, s>>>(w.partial, PSD_BLOCKS, w.sums);
+  psd_rescale_kernel<<<blocks, 256, 0, s>>>(out, NN, w.sums, rms);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }

@@ -1,6 +1,14 @@
-"""Wavefront-error and source-spectrum generators (host-side numpy, input
-preparation only)."""
+"""Wavefront-error and source-spectrum generators.
+
+``power_spectrum`` filters seeded white noise on the GPU
+(``lgb_power_spectrum``); the noise itself is drawn with numpy's generator
+from the same seed so that the surface matches lentil's.  The blackbody
+weights are a few host-side numbers."""
 import numpy as np
+import torch
+
+from . import _device as dv
+from . import _lib
 
 # lentil/radiometry.py:12-14
 _H = 6.62606957e-34
@@ -10,22 +18,21 @@ _K = 1.3806488e-23
 
 def power_spectrum(mask, pixelscale, rms, half_power_freq, exp, seed=None):
     """Seeded 1/f^exp surface error, masked and scaled to ``rms`` over the
-    nonzero pixels (lentil/wfe.py:8-70; Sidick 2009 PSD filter)."""
-    mask = np.asarray(mask)
+    nonzero pixels (lentil/wfe.py:8-70; Sidick 2009 PSD filter).  lentil's
+    frequency grid is only consistent for square masks; numpy masks give a
+    numpy OPD, CUDA tensors a CUDA tensor."""
+    n, m = (int(x) for x in (mask.shape if dv.is_tensor(mask) else np.shape(mask)))
+    if n != m:
+        raise ValueError(f'power_spectrum needs a square mask, got {(n, m)}')
     rng = np.random.default_rng(seed)
-    n, m = mask.shape
-    fy = (np.arange(m) - (np.floor(m / 2) + 1)) / m
-    fx = (np.arange(n) - (np.floor(n / 2) + 1)) / n
-    dr = np.hypot(fy[:, None], fx[None, :])
-    f0 = half_power_freq * pixelscale / np.sqrt(m ** 2 + n ** 2)
-    psd = 1.0 / (1.0 + (dr / f0) ** exp)
-    psd[dr == 0] = 0
-    psd = psd / psd.sum()
-    filt = np.fft.fftshift(np.sqrt(psd))
-    noise = rng.normal(size=[n, m])
-    opd = np.real(np.fft.ifft2(np.fft.fft2(noise) * filt)) * np.sqrt(m * n)
-    opd = opd * mask
-    return opd * np.sqrt(np.count_nonzero(opd) / np.sum(np.abs(opd) ** 2)) * rms
+    noise = dv.to_device(rng.normal(size=[n, m]), torch.float64)
+    mask_d = dv.to_device(mask, torch.float64)
+    out = torch.empty((n, m), dtype=torch.float64, device=noise.device)
+    ws = dv.workspace(_lib.load().lgb_power_spectrum_workspace_size(n))
+    _lib.call('lgb_power_spectrum', noise.data_ptr(), mask_d.data_ptr(), n, float(pixelscale),
+              float(rms), float(half_power_freq), float(exp), out.data_ptr(), ws.data_ptr(),
+              ws.numel(), dv.stream_ptr())
+    return out if dv.is_tensor(mask) else dv.to_host(out)
 
 
 def blackbody_photlam(wave_nm, temp):

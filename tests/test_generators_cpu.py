@@ -67,9 +67,3 @@ def test_zernike_radial_terms_match_lentil():
             got = sum(a * rho ** p for a, p in lz.radial_terms(n, m)) if lz.radial_terms(n, m) else 0
             assert np.array_equal(np.asarray(got), np.asarray(want)), (n, m)
 
-
-def test_power_spectrum_golden(golden):
-    # host-side input generator of lentil_gb300 (seeded numpy noise, as lentil)
-    g = golden('generators')
-    psd = lg.power_spectrum(lg.circle((64, 64), 30), 1 / 64, 25e-9, 8, 2, seed=7)
-    assert np.max(np.abs(psd - g['psd'])) <= 1e-12 * np.max(np.abs(g['psd']))

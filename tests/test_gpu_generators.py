@@ -83,3 +83,27 @@ def test_zernike_tensor_in_tensor_out(cuda_device):
 def test_zernike_empty_mask_raises(cuda_device):
     with pytest.raises(ValueError):
         lg.zernike_coordinates(np.zeros((16, 16)))
+
+
+def test_power_spectrum_golden(golden, cuda_device):
+    # 64 x 64: the radix-2 FFT path
+    g = golden('generators')
+    psd = lg.power_spectrum(lg.circle((64, 64), 30), 1 / 64, 25e-9, 8, 2, seed=7)
+    _close(psd, g['psd'])
+
+
+@pytest.mark.parametrize('N', [90, 256])
+def test_power_spectrum_vs_oracle(cuda_device, N):
+    # 90: DFT-matrix path (not a power of two); 256: FFT path
+    mask = lg.circle((N, N), 0.45 * N)
+    _close(lg.power_spectrum(mask, 1 / N, 20e-9, 10.0, 2.5, seed=N),
+           lo.power_spectrum(mask, 1 / N, 20e-9, 10.0, 2.5, seed=N))
+
+
+def test_power_spectrum_tensor_and_errors(cuda_device):
+    mask = torch.as_tensor(lg.circle((32, 32), 14), device='cuda')
+    z = lg.power_spectrum(mask, 1 / 32, 10e-9, 5.0, 2, seed=1)
+    assert isinstance(z, torch.Tensor) and z.is_cuda
+    _close(z.cpu().numpy(), lo.power_spectrum(mask.cpu().numpy(), 1 / 32, 10e-9, 5.0, 2, seed=1))
+    with pytest.raises(ValueError):
+        lg.power_spectrum(np.ones((16, 20)), 1 / 16, 1e-8, 4.0, 2, seed=0)

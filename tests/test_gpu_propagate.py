@@ -232,3 +232,26 @@ def test_large_oversampled_pixelated_small_scale(cuda_device, precision, tol):
                                                 precision=precision, **kw), 4)
     assert img.shape == ref.shape == (64, 64)
     assert lo.peak_normalised_error(img, ref) < tol
+
+
+def test_image_to_pupil_round_trip(cuda_device):
+    # pupil -> image -> field stop (Image plane) -> propagate_dft back to a
+    # pupil plane (lentil/propagate.py:263-272 flips the ptype), complex128,
+    # against the oracle at every plane
+    rng = np.random.default_rng(17)
+    amp = lg.normalize_power(lg.circle((96, 96), 44))
+    opd = lg.zernike_compose(amp > 0, np.r_[0, rng.normal(0, 40e-9, 10)])
+    stop = lg.circle((64, 64), 20)
+    out = {}
+    for mod in (lg, lo):
+        pl = mod.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 96, focal_length=10)
+        w = mod.propagate_dft(mod.Wavefront(700e-9) * pl, pixelscale=8e-6, shape=32, oversample=2)
+        assert w.ptype == (lg.image if mod is lg else lo.IMAGE)
+        w = mod.Image(amplitude=stop, pixelscale=4e-6) * w
+        back = mod.propagate_dft(w, pixelscale=1 / 96, shape=96, oversample=1)
+        assert back.ptype == (lg.pupil if mod is lg else lo.PUPIL)
+        f = back.field
+        out[mod.__name__] = f.cpu().numpy() if isinstance(f, torch.Tensor) else np.asarray(f)
+    got, ref = out['lentil_gb300'], out[lo.__name__]
+    assert got.shape == ref.shape == (96, 96)
+    assert lo.peak_normalised_error(got, ref) < 1e-12
