@@ -96,7 +96,9 @@ def run_reference(args):
     if rank != 0:
         return
     from lentil_gb300 import workloads
-    wl = workloads.broadband_segmented(args.npix, args.wavelengths)
+    from oracle import lentil_oracle as lo
+    # the same seeded workload, its Zernike modes evaluated on the host
+    wl = workloads.broadband_segmented(args.npix, args.wavelengths, basis=lo.zernike_basis)
     opd = wl.opds(1)[0]
     n = max(1, args.cpu_lambdas)
     for _ in range(args.warmup if args.warmup < 1 else 1):

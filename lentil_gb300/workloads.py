@@ -51,32 +51,36 @@ class Workload:
         return out.astype(np.float64)
 
 
-def broadband_segmented(npix=1024, n_wavelengths=64, seed=2, seg_radius=None):
-    """The broadband segmented workload (see module docstring)."""
+def broadband_segmented(npix=1024, n_wavelengths=64, seed=2, seg_radius=None, basis=None):
+    """The broadband segmented workload (see module docstring).  ``basis``
+    evaluates Zernike modes (``zernike_basis`` signature); the default runs
+    on the GPU, a host implementation can stand in where no GPU is used."""
+    basis = zernike_basis if basis is None else basis
     if seg_radius is None:
         seg_radius = 116.8 * npix / 1024
     segs = shapes.hex_segments(rings=2, seg_radius=seg_radius, seg_gap=2)
     segs = np.asarray([util.pad(s, (npix, npix)) for s in segs])
     gmask = segs.sum(axis=0)
     amp = util.normalize_power(gmask)
-    basis, sigma = [], []
+    modes, sigma = [], []
     for s in segs:                                # piston, tip, tilt of each segment
-        basis.extend(zernike_basis(s, [1, 2, 3]).astype(np.float32))
+        modes.extend(np.asarray(basis(s, [1, 2, 3]), dtype=np.float32))
         sigma.extend([50e-9] * 3)
-    basis.extend(zernike_basis(gmask, range(2, 23)).astype(np.float32))   # global Noll 2-22
+    modes.extend(np.asarray(basis(gmask, list(range(2, 23))), dtype=np.float32))  # Noll 2-22
     sigma.extend([15e-9] * 21)
     wl_nm = np.linspace(500.0, 900.0, n_wavelengths)
     w = blackbody_photlam(wl_nm, 5800.0)
-    return Workload('broadband_segmented', amp, segs, np.asarray(basis), np.asarray(sigma),
+    return Workload('broadband_segmented', amp, segs, np.asarray(modes), np.asarray(sigma),
                     wl_nm * 1e-9, w / w.sum(), 1.0 / npix, 10.0, 5e-6, npix // 2, 2, seed)
 
 
-def monochromatic_circle(seed=1):
+def monochromatic_circle(seed=1, basis=None):
     """The monochromatic circular-pupil workload (see module docstring)."""
+    basis = zernike_basis if basis is None else basis
     npix = 256
     amp = util.normalize_power(shapes.circle((npix, npix), npix // 2, antialias=False))
-    basis = zernike_basis(amp, range(2, 12)).astype(np.float32)
-    return Workload('monochromatic_circle', amp, None, basis, np.full(10, 20e-9),
+    modes = np.asarray(basis(amp, list(range(2, 12))), dtype=np.float32)
+    return Workload('monochromatic_circle', amp, None, modes, np.full(10, 20e-9),
                     np.array([650e-9]), np.array([1.0]), 1.0 / npix, 10.0, 5e-6, 128, 2, seed)
 
 
