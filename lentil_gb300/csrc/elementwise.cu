@@ -111,13 +111,19 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
       const float2 kk = a.khalf[a.lam_idx ? a.lam_idx[l] : l];   // 2/lambda, float-float pair
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        // x = opd * 2/lambda half-cycles, reduced mod 2 before sincospi
+        // x = opd * 2/lambda half-cycles, reduced mod 2 before the sine
         const float p = o_hi[k] * kk.x;
         float e = fmaf(o_hi[k], kk.x, -p);
         e = fmaf(o_hi[k], kk.y, fmaf(o_lo[k], kk.x, e));
         const float x = (p - 2.f * rintf(0.5f * p)) + e;
         float sn, cs;
-        sincospif(x, &sn, &cs);
+        if (BF16) {
+          // bf16 hi+lo keeps ~16 significant bits (error ~2^-17); the SFU
+          // sine's absolute error on [-pi, pi] (~2^-21.4) is far below that
+          __sincosf(x * 3.14159265358979f, &sn, &cs);
+        } else {
+          sincospif(x, &sn, &cs);        // fp16 hi+lo keeps ~22 bits
+        }
         fv[k] = make_float2(amp_r[k] * cs, amp_r[k] * sn);
       }
     }

@@ -81,6 +81,7 @@ struct Params {
   uint32_t idesc;
   int M, N;                  // stage 1: rows of G / stage 2: window shape
   int kp_out;                // stage 1: row half-width of G (kp2)
+  int n_last;                // MMA N of the last column tile (<= 256, multiple of 32)
   float sG;                  // stage-2 operand scale (power of two)
   uint16_t* g_hi;
   uint16_t* g_lo;
@@ -95,6 +96,13 @@ struct Params {
   int* err;
   const int* lam_idx;        // [L] wavelength -> DFT-matrix slot, or null (identity)
 };
+
+// MMA N of column tile tn: 256, except a narrower last tile when the
+// operand's columns end inside it (no MMA work on padding columns).  The
+// pair splits a tile's B rows evenly: CTA r holds rows r*N/2 .. of it.
+__device__ __forceinline__ int tile_n(const Params& p, int tn) {
+  return tn == p.n_tiles - 1 ? p.n_last : BN;
+}
 
 __device__ __forceinline__ int matrix_slot(const Params& p, int lam) {
   return p.lam_idx ? p.lam_idx[lam] : lam;
@@ -468,7 +476,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
         const int az = p.stage == 1 ? matrix_slot(p, w.lam) : w.q;
         const int bz = p.stage == 1 ? w.q : matrix_slot(p, w.lam);
         const int ay = (2 * w.tm + (int)rank) * BM;
-        const int by = w.tn * BN + (int)rank * BNC;
+        const int by = w.tn * BN + (int)rank * (tile_n(p, w.tn) >> 1);
         for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
           const int s = it % STAGES;
           if (!mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1, p.err)) { ok = false; break; }
@@ -493,6 +501,8 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
       uint32_t it = 0;                       // K blocks issued (also accumulator uses)
       bool ok = true;
       for (int i = pair; ok && i < p.n_items; i += npairs) {
+        const uint32_t idesc = (p.idesc & ~(0x3Fu << 17)) |
+                               ((uint32_t)(tile_n(p, decode(p, i).tn) >> 3) << 17);
         for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
           const int s = it % STAGES, xb = it & 1;
           if (!mbar_wait(full_bar(s), (it / STAGES) & 1, p.err)) { ok = false; break; }
@@ -503,13 +513,13 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
 #pragma unroll
           for (int k = 0; k < KSTEPS; ++k) {     // hi.lo + lo.hi: small terms first
             mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + B_BYTES + k * 32),
-                    p.idesc, k ? 1u : 0u);
+                    idesc, k ? 1u : 0u);
             mma_f16(X, smem_desc(sa + A_BYTES + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32),
-                    p.idesc, 1u);
+                    idesc, 1u);
           }
 #pragma unroll
           for (int k = 0; k < KSTEPS; ++k)       // hi.hi last
-            mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32), p.idesc, 1u);
+            mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32), idesc, 1u);
           mma_commit_pair(empty_bar(s));         // both CTAs' stage s free once these retire
           mma_commit_pair(acc_full(xb));         // accumulator xb ready for the epilogues
         }
@@ -704,6 +714,7 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   p.idesc = idesc;
   p.M = q.M; p.N = q.N;
   p.kp_out = q.kp2;
+  p.n_last = q.kp2 - (p.n_tiles - 1) * BN;              // kp2 % 32 == 0, so n_last % 32 == 0
   p.sG = split_g_scale(q.m);
   p.g_hi = q.g_hi; p.g_lo = q.g_lo;
   p.maxabs = q.maxabs;
@@ -730,6 +741,7 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   p.kblocks = 2 * q.kp2 / BK;
   p.m_tiles = cdiv(q.M, 2 * BM);
   p.n_tiles = cdiv(q.N, 128);
+  p.n_last = BN;                                        // E2 blocks are padded to whole tiles
   p.n_items = Q * p.m_tiles * p.n_tiles;
   p.epilogue = q.epilogue;
   p.weights = q.weights;
