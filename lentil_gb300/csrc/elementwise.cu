@@ -168,9 +168,24 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
   const int spatial = cdiv(a.kp, TR) * cdiv(a.n, TC);
   const int psfs = a.amp ? a.batch : 1;
   const int L = a.amp ? a.L : 1;
-  // enough blocks for ~8 resident per SM, no group smaller than one wavelength
-  int groups = cdiv(8 * sm_count(), std::max(1, spatial * psfs));
-  groups = std::max(1, std::min(groups, L));
+  // Wavelength groups: each group re-reads the block's amp/opd once, and
+  // the blocks run in waves of `cap` resident blocks; pick the group count
+  // that minimises whole waves per wavelength of work (the last wave of a
+  // launch is otherwise partly empty), among counts up to 16.
+  int per_sm = 0;
+  auto kfn = bf16 ? (a.amp ? split_field_T_kernel<true, true> : split_field_T_kernel<true, false>)
+                  : (a.amp ? split_field_T_kernel<false, true> : split_field_T_kernel<false, false>);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, 0) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const long long cap = (long long)per_sm * sm_count();
+  const long long base = std::max(1LL, (long long)spatial * psfs);
+  int groups = 1;
+  double best = 1e300;
+  for (int g = 1; g <= std::min(L, 16); ++g) {
+    const long long waves = (base * g + cap - 1) / cap;
+    const double cost = (double)waves * (double)cdiv(L, g);    // waves x wavelengths per block
+    if (cost < best * (1.0 - 1e-9)) { best = cost; groups = g; }
+  }
   groups = cdiv(L, cdiv(L, groups));                 // no empty trailing group
   LGB_REQUIRE((long long)psfs * groups <= 65535, LGB_EINVAL, "split field: too many PSFs in one launch");
   dim3 grid(cdiv(a.kp, TR), cdiv(a.n, TC), psfs * groups);
