@@ -196,6 +196,20 @@ class ClockSampler:
                 'window_s': self.t_out - self.t_in}
 
 
+def slowest_rank(ms_local, units_per_rank, world, device):
+    """Whole-job throughput of independent replicas: the slowest rank's time
+    (MAX over ranks) and the units all ranks processed in it.  The path has
+    no data exchange; the one collective is this reduction of the clock."""
+    ms = float(ms_local)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * units_per_rank / (ms / 1e3)
+
+
 def peaks():
     try:
         with open(PEAKS_FILE) as fh:
@@ -279,13 +293,8 @@ def run_gpu(args):
     kcnt = (ctypes.c_int * 4)()
     _lib.call('lgb_psf_plan_kernel_times', plan._h, kms, kcnt, 4)
     _lib.call('lgb_psf_plan_status', plan._h, stream.cuda_stream)
-    total_ms = t_start.elapsed_time(t_end)
     step_ms = sorted(a.elapsed_time(b) for a, b in ev)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * B * args.steps / (total_ms / 1e3)
+    total_ms, value = slowest_rank(t_start.elapsed_time(t_end), B * args.steps, world, dev)
 
     # ---------------- end-to-end through the plan with host buffers --------
     # Every step copies its amp/opd/weights from pinned host memory and reads
@@ -339,11 +348,7 @@ def run_gpu(args):
     barrier()
     if not torch.equal(hOut[(args.steps - 1) & 1], dOut[(args.steps - 1) & 1].cpu()):
         raise RuntimeError('end-to-end image read back differs from the device image')
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * B * args.steps / (e2e_ms / 1e3)
+    e2e_ms, e2e_value = slowest_rank(e2e_ms, B * args.steps, world, dev)
     h2d = (A.numel() + O.numel() + Wt.numel()) * 8
     d2h = out.numel() * 8
 
