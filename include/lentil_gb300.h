@@ -73,6 +73,17 @@ int lgb_dft2(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int N,
  * for the stream.  LGB_ETIMEOUT if a tensor-core pipeline wait expired. */
 int lgb_dft2_status(void* workspace, lgb_stream stream);
 
+/* Batched dft2 (an extension; lentil's dft2 transforms one array): `count`
+ * fields f[count][m][n] with one geometry -> F[count][M][N]; the DFT
+ * matrices are built once and the split path transforms the whole batch in
+ * one pair of tensor-core launches.  lgb_dft2 is the count == 1 case.
+ * Workspace: lgb_dft2_batch_workspace_size(count, ...) bytes. */
+size_t lgb_dft2_batch_workspace_size(int count, int m, int n, int M, int N, int precision);
+int lgb_dft2_batch(const lgb_c128* f, int count, int m, int n, lgb_c128* F, int M, int N,
+                   double alpha_r, double alpha_c, double shift_r, double shift_c,
+                   double offset_r, double offset_c, int unitary, int precision,
+                   void* workspace, size_t workspace_bytes, lgb_stream stream);
+
 /* ------------------------------------------------------------------------
  * Allocation-free complex128 dft2 (no counterpart in lentil: an addition of
  * this library for callers that may not allocate device memory at call time,

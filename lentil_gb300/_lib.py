@@ -41,6 +41,10 @@ SIGNATURES = {
                          c_double, c_double, c_double, c_double, c_int, c_int, c_void_p, c_size_t,
                          c_void_p]),
     'lgb_dft2_status': (c_int, [c_void_p, c_void_p]),
+    'lgb_dft2_batch_workspace_size': (c_size_t, [c_int, c_int, c_int, c_int, c_int, c_int]),
+    'lgb_dft2_batch': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_int, c_double,
+                               c_double, c_double, c_double, c_double, c_double, c_int, c_int,
+                               c_void_p, c_size_t, c_void_p]),
     'lgb_dft2_noalloc': (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double,
                                  c_double, c_double, c_double, c_double, c_double, c_int,
                                  c_void_p]),

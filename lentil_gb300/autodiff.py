@@ -52,46 +52,56 @@ def _phasor(amp, opd, g):
 
 
 def _forward_field(amp, opd, g):
-    f = _phasor(amp, opd, g)
-    F = fourier.dft2(f, g.alpha, shape=g.shape, shift=g.shift, offset=g.offset, unitary=True,
-                     precision=g.precision)
+    """Fields f [K, m, n] of a stack of OPD maps opd [K, H, W] and their
+    transforms F [K, M, N] (one batched MFT for the whole stack)."""
+    f = torch.stack([_phasor(amp, o, g) for o in opd])
+    F = fourier.dft2_batch(f, g.alpha, shape=g.shape, shift=g.shift, offset=g.offset,
+                           unitary=True, precision=g.precision)
     return f, F
 
 
 class MFTIntensity(torch.autograd.Function):
-    """I = |dft2(amp exp(2 pi i opd / lambda))|^2, differentiable in opd."""
+    """I = |dft2(amp exp(2 pi i opd / lambda))|^2, differentiable in opd.
+    ``opd`` is one map [H, W] or a stack [K, H, W] sharing ``amp`` and the
+    geometry (e.g. focus-diverse images); the stack is transformed in one
+    batched MFT, forward and backward."""
 
     @staticmethod
     def forward(ctx, opd, amp, g):
+        single = opd.dim() == 2
         opd = opd.detach().to(torch.float64).contiguous()
+        opd = opd.unsqueeze(0) if single else opd
         amp = amp.detach().to(torch.float64).contiguous()
         _, F = _forward_field(amp, opd, g)
         I = torch.empty(F.shape, dtype=torch.float64, device=F.device)
         _lib.call('lgb_abs2', F.data_ptr(), I.data_ptr(), F.numel(), dv.stream_ptr())
         ctx.save_for_backward(opd, amp)
-        ctx.g = g
-        return I
+        ctx.g, ctx.single = g, single
+        return I[0] if single else I
 
     @staticmethod
     def backward(ctx, grad_I):
         opd, amp = ctx.saved_tensors
         g = ctx.g
         f, F = _forward_field(amp, opd, g)                 # recomputed, not stored
-        gI = grad_I.detach().to(torch.float64).contiguous()
+        gI = grad_I.detach().to(torch.float64).contiguous().reshape(F.shape)
         Hc = torch.empty_like(F)
         _lib.call('lgb_intensity_adjoint', F.data_ptr(), gI.data_ptr(), Hc.data_ptr(), F.numel(),
                   dv.stream_ptr())
         r0, c0, m, n = g.slc
-        q = fourier.dft2(Hc, g.alpha, shape=(m, n), shift=(-g.offset[0], -g.offset[1]),
-                         offset=(-g.shift[0], -g.shift[1]), unitary=True, precision=g.precision)
+        q = fourier.dft2_batch(Hc, g.alpha, shape=(m, n), shift=(-g.offset[0], -g.offset[1]),
+                               offset=(-g.shift[0], -g.shift[1]), unitary=True,
+                               precision=g.precision)
         grad = torch.zeros_like(opd)
-        _lib.call('lgb_phasor_adjoint', q.data_ptr(), f.data_ptr(), m, n, g.wavelength,
-                  grad.data_ptr(), g.plane[1], r0, c0, dv.stream_ptr())
-        return grad, None, None
+        for k in range(opd.shape[0]):
+            _lib.call('lgb_phasor_adjoint', q[k].data_ptr(), f[k].data_ptr(), m, n, g.wavelength,
+                      grad[k].data_ptr(), g.plane[1], r0, c0, dv.stream_ptr())
+        return (grad[0] if ctx.single else grad), None, None
 
 
 def mft_intensity(opd, amp, g):
-    """Differentiable PSF intensity of ``amp * exp(2 pi i opd / lambda)``."""
+    """Differentiable PSF intensity of ``amp * exp(2 pi i opd / lambda)``
+    for one OPD map or a stack of them."""
     return MFTIntensity.apply(opd, amp, g)
 
 
@@ -115,7 +125,5 @@ class PhaseRetrieval:
 
     def loss(self, coeffs, free=None):
         o = self.opd(coeffs, free)
-        total = 0.0
-        for d, t in zip(self.diversity, self.targets):
-            total = total + ((mft_intensity(o + d, self.amp, self.g) - t) ** 2).sum()
-        return total
+        stack = o.unsqueeze(0) + torch.stack(self.diversity)   # all images in one batched MFT
+        return ((mft_intensity(stack, self.amp, self.g) - torch.stack(self.targets)) ** 2).sum()

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
         o_hi[k] = (float)o;
         o_lo[k] = (float)(o - (double)o_hi[k]);
       } else {
-        const double2 v = a.field[(size_t)r * a.n + c];
+        const double2 v = a.field[((size_t)b * a.m + r) * a.n + c];
         fv[k] = make_float2((float)v.x * sf, (float)v.y * sf);
       }
     }
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
 
 int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
   const int spatial = cdiv(a.kp, TR) * cdiv(a.n, TC);
-  const int psfs = a.amp ? a.batch : 1;
+  const int psfs = a.batch;
   const int L = a.amp ? a.L : 1;
   // Wavelength groups: each group re-reads the block's amp/opd once, and
   // the blocks run in waves of `cap` resident blocks; pick the group count
@@ -225,6 +225,8 @@ __global__ void maxabs_amp_kernel(const double* __restrict__ amp, int H, int W, 
 
 __global__ void maxabs_c128_kernel(const double2* __restrict__ f, int count, float* __restrict__ out) {
   float v = 0.f;
+  f += (size_t)blockIdx.y * count;                 // field blockIdx.y of a batch
+  out += blockIdx.y;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x) {
     const double2 z = f[p];
     v = fmaxf(v, fmaxf((float)fabs(z.x), (float)fabs(z.y)));
@@ -243,9 +245,13 @@ int launch_maxabs_amp(const double* amp, int batch, int H, int W, int r0, int c0
 }
 
 int launch_maxabs_c128(const double2* f, int count, float* out, cudaStream_t s) {
-  LGB_CUDA(cudaMemsetAsync(out, 0, sizeof(float), s));
+  return launch_maxabs_c128_batch(f, count, 1, out, s);
+}
+
+int launch_maxabs_c128_batch(const double2* f, int count, int batch, float* out, cudaStream_t s) {
+  LGB_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * batch, s));
   const int blocks = std::max(1, std::min(2 * sm_count(), cdiv(count, 256)));
-  maxabs_c128_kernel<<<blocks, 256, 0, s>>>(f, count, out);
+  maxabs_c128_kernel<<<dim3(blocks, batch), 256, 0, s>>>(f, count, out);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }

@@ -32,7 +32,7 @@ struct SplitFieldArgs {
   int H, W, r0, c0;
   const float2* khalf;     // [L] (hi, lo) float pair of 2/lambda
   // complex mode
-  const double2* field;    // [m][n] complex128 (batch 1, L 1)
+  const double2* field;    // [batch][m][n] complex128 (L 1)
   // common
   int m, n, kp, L, batch;
   const float* maxabs;     // [batch] max |component| of the field (device)
@@ -46,6 +46,8 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s);
 int launch_maxabs_amp(const double* amp, int batch, int H, int W, int r0, int c0, int m, int n,
                       float* out, cudaStream_t s);
 int launch_maxabs_c128(const double2* f, int count, float* out, cudaStream_t s);
+// per field b < batch of `count` entries each: out[b] = max(|re|, |im|)
+int launch_maxabs_c128_batch(const double2* f, int count, int batch, float* out, cudaStream_t s);
 
 // out[i,j] (+)= (re, im) scaled; generic complex128 copy/convert kernels
 int launch_conj_scale(const double2* in, double2* out, size_t count, double scale, cudaStream_t s);
@@ -83,7 +85,7 @@ struct SplitMftProblem {
   const double* unit2;     // [L] |alpha_r alpha_c| (or 1)
   float* wbuf;             // intensity: [batch][M][ldw] FP32 window, zeroed by the caller
   int ldw;                 // multiple of 4
-  double* out;             // complex: [M][N] double2
+  double* out;             // complex: [batch * L][M][N] double2
   double complex_scale;    // complex epilogue: extra scale (unitary factor)
   int* err;                // device error flag
   cudaEvent_t* events;     // optional [4]: recorded around the stage-1 and stage-2 launches

@@ -91,7 +91,7 @@ struct Params {
   const double* unit2;       // [L]
   float* wbuf;               // stage 2 intensity: [batch][M][ldw] FP32 window
   int ldw;
-  double* out;               // stage 2 complex: [M][N] complex128
+  double* out;               // stage 2 complex: [Q][M][N] complex128
   double cscale;
   int* err;
   const int* lam_idx;        // [L] wavelength -> DFT-matrix slot, or null (identity)
@@ -408,7 +408,7 @@ __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int
   } else {
     if (u >= p.M) return;
     const double scl = p.cscale / ((double)sf * (double)p.sG);
-    double2* outc = reinterpret_cast<double2*>(p.out) + (size_t)u * p.N;
+    double2* outc = reinterpret_cast<double2*>(p.out) + ((size_t)w.q * p.M + u) * p.N;
 #pragma unroll
     for (int j = 0; j < 64; ++j)
       if (v0 + j < p.N) outc[v0 + j] = make_double2(scl * run[j], scl * run[64 + j]);

@@ -44,32 +44,32 @@ struct Dft2SplitSpace {
   uint16_t *e1h, *e1l, *fh, *fl, *gh, *gl, *e2h, *e2l;
 };
 
-static size_t carve_fp64(void* ws, int m, int n, int M, int N, Dft2Fp64Space* s) {
+static size_t carve_fp64(void* ws, int count, int m, int n, int M, int N, Dft2Fp64Space* s) {
   Carve c(ws);
   Dft2Fp64Space t;
   t.err = c.take<int>(4);
   t.E1 = c.take<double2>((size_t)M * m);
   t.E2 = c.take<double2>((size_t)n * N);
-  t.T = c.take<double2>(std::max((size_t)M * n, (size_t)m * N));
+  t.T = c.take<double2>((size_t)count * std::max((size_t)M * n, (size_t)m * N));
   if (s) *s = t;
   return c.used;
 }
 
-static size_t carve_split(void* ws, int m, int n, int M, int N, Dft2SplitSpace* s) {
+static size_t carve_split(void* ws, int count, int m, int n, int M, int N, Dft2SplitSpace* s) {
   const int kp1 = round_up(m, 32), kp2 = round_up(n, 32);
   const size_t mrows1 = (size_t)cdiv(M, 64) * 128, nrows2 = (size_t)cdiv(N, 128) * 256;
   Carve c(ws);
   Dft2SplitSpace t;
   t.err = c.take<int>(4);
   t.axes = c.take<PhaseAxis>(2);
-  t.maxabs = c.take<float>(4);
+  t.maxabs = c.take<float>(std::max(count, 4));
   t.unit2 = c.take<double>(2);
   t.e1h = c.take<uint16_t>(mrows1 * 2 * kp1);
   t.e1l = c.take<uint16_t>(mrows1 * 2 * kp1);
-  t.fh = c.take<uint16_t>((size_t)n * 2 * kp1);
-  t.fl = c.take<uint16_t>((size_t)n * 2 * kp1);
-  t.gh = c.take<uint16_t>((size_t)M * 2 * kp2);
-  t.gl = c.take<uint16_t>((size_t)M * 2 * kp2);
+  t.fh = c.take<uint16_t>((size_t)count * n * 2 * kp1);
+  t.fl = c.take<uint16_t>((size_t)count * n * 2 * kp1);
+  t.gh = c.take<uint16_t>((size_t)count * M * 2 * kp2);
+  t.gl = c.take<uint16_t>((size_t)count * M * 2 * kp2);
   t.e2h = c.take<uint16_t>(nrows2 * 2 * kp2);
   t.e2l = c.take<uint16_t>(nrows2 * 2 * kp2);
   if (s) *s = t;
@@ -87,24 +87,31 @@ static int check_sizes(int m, int n, int M, int N) {
 
 using namespace lgb;
 
-extern "C" size_t lgb_dft2_workspace_size(int m, int n, int M, int N, int precision) {
-  if (m <= 0 || n <= 0 || M <= 0 || N <= 0) return 0;
-  return is_split(precision) ? carve_split(nullptr, m, n, M, N, nullptr)
-                             : carve_fp64(nullptr, m, n, M, N, nullptr);
+extern "C" size_t lgb_dft2_batch_workspace_size(int count, int m, int n, int M, int N,
+                                                int precision) {
+  if (count <= 0 || m <= 0 || n <= 0 || M <= 0 || N <= 0) return 0;
+  return is_split(precision) ? carve_split(nullptr, count, m, n, M, N, nullptr)
+                             : carve_fp64(nullptr, count, m, n, M, N, nullptr);
 }
 
-extern "C" int lgb_dft2(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int N,
-                        double alpha_r, double alpha_c, double shift_r, double shift_c,
-                        double offset_r, double offset_c, int unitary, int precision,
-                        void* workspace, size_t workspace_bytes, lgb_stream stream) {
+extern "C" size_t lgb_dft2_workspace_size(int m, int n, int M, int N, int precision) {
+  return lgb_dft2_batch_workspace_size(1, m, n, M, N, precision);
+}
+
+extern "C" int lgb_dft2_batch(const lgb_c128* f, int count, int m, int n, lgb_c128* F, int M,
+                              int N, double alpha_r, double alpha_c, double shift_r,
+                              double shift_c, double offset_r, double offset_c, int unitary,
+                              int precision, void* workspace, size_t workspace_bytes,
+                              lgb_stream stream) {
   int st = check_sizes(m, n, M, N);
   if (st) return st;
+  LGB_REQUIRE(count >= 1 && count <= 65535, LGB_EINVAL, "dft2: count outside 1..65535");
   LGB_REQUIRE(f && F, LGB_EINVAL, "dft2: null input or output");
   LGB_REQUIRE(precision == LGB_FP64 || is_split(precision), LGB_EINVAL, "dft2: unknown precision");
   LGB_REQUIRE(workspace && ((uintptr_t)workspace & 255) == 0, LGB_EWORKSPACE,
               "dft2: workspace must be non-null and 256-byte aligned");
-  LGB_REQUIRE(workspace_bytes >= lgb_dft2_workspace_size(m, n, M, N, precision), LGB_EWORKSPACE,
-              "dft2: workspace too small");
+  LGB_REQUIRE(workspace_bytes >= lgb_dft2_batch_workspace_size(count, m, n, M, N, precision),
+              LGB_EWORKSPACE, "dft2: workspace too small");
   PhaseAxis ar, ac;
   if ((st = make_phase_axis(alpha_r, shift_r, offset_r, m, M, &ar))) return st;
   if ((st = make_phase_axis(alpha_c, shift_c, offset_c, n, N, &ac))) return st;
@@ -115,42 +122,46 @@ extern "C" int lgb_dft2(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int
 
   if (precision == LGB_FP64) {
     Dft2Fp64Space w;
-    carve_fp64(workspace, m, n, M, N, &w);
+    carve_fp64(workspace, count, m, n, M, N, &w);
     LGB_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), s));
     if ((st = launch_dft_matrix_c128(ar, m, M, w.E1, true, s))) return st;
     if ((st = launch_dft_matrix_c128(ac, n, N, w.E2, false, s))) return st;
-    // (E1 f) E2 as lentil, or E1 (f E2) when that order needs fewer flops
+    // (E1 f) E2 as lentil, or E1 (f E2) when that order needs fewer flops;
+    // the matrices are shared by the batch (stride 0)
+    const long long sf = (long long)m * n, sF = (long long)M * N;
     const double cost_left = (double)M * m * n + (double)M * n * N;
     const double cost_right = (double)m * n * N + (double)M * m * N;
     if (cost_left <= cost_right) {
-      if ((st = launch_zgemm(M, n, m, w.E1, m, 0, fin, n, 0, w.T, n, 0, 1, 1.0, s))) return st;
-      return launch_zgemm(M, N, n, w.T, n, 0, w.E2, N, 0, Fout, N, 0, 1, scale, s);
+      const long long sT = (long long)M * n;
+      if ((st = launch_zgemm(M, n, m, w.E1, m, 0, fin, n, sf, w.T, n, sT, count, 1.0, s))) return st;
+      return launch_zgemm(M, N, n, w.T, n, sT, w.E2, N, 0, Fout, N, sF, count, scale, s);
     }
-    if ((st = launch_zgemm(m, N, n, fin, n, 0, w.E2, N, 0, w.T, N, 0, 1, 1.0, s))) return st;
-    return launch_zgemm(M, N, m, w.E1, m, 0, w.T, N, 0, Fout, N, 0, 1, scale, s);
+    const long long sT = (long long)m * N;
+    if ((st = launch_zgemm(m, N, n, fin, n, sf, w.E2, N, 0, w.T, N, sT, count, 1.0, s))) return st;
+    return launch_zgemm(M, N, m, w.E1, m, 0, w.T, N, sT, Fout, N, sF, count, scale, s);
   }
 
-  // split precision on the tensor cores
+  // split precision on the tensor cores: one launch pair for the whole batch
   const bool bf16 = precision == LGB_SPLIT_BF16;
   const int kp1 = round_up(m, 32), kp2 = round_up(n, 32);
   Dft2SplitSpace w;
-  carve_split(workspace, m, n, M, N, &w);
+  carve_split(workspace, count, m, n, M, N, &w);
   PhaseAxis axes[2] = {ar, ac};
   LGB_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), s));
   LGB_CUDA(cudaMemcpyAsync(w.axes, axes, sizeof(axes), cudaMemcpyHostToDevice, s));
   if ((st = launch_e1_block_split(w.axes, 1, m, M, kp1, cdiv(M, 64) * 128, bf16, w.e1h, w.e1l, s))) return st;
   if ((st = launch_e2_block_split(w.axes + 1, 1, n, N, kp2, cdiv(N, 128) * 256, bf16, w.e2h, w.e2l, s))) return st;
-  if ((st = launch_maxabs_c128(fin, m * n, w.maxabs, s))) return st;
+  if ((st = launch_maxabs_c128_batch(fin, m * n, count, w.maxabs, s))) return st;
   SplitFieldArgs fa{};
   fa.field = fin;
-  fa.m = m; fa.n = n; fa.kp = kp1; fa.L = 1; fa.batch = 1;
+  fa.m = m; fa.n = n; fa.kp = kp1; fa.L = 1; fa.batch = count;
   fa.maxabs = w.maxabs;
   fa.hi = w.fh; fa.lo = w.fl;
   if ((st = launch_split_field_T(fa, bf16, s))) return st;
   const double one = 1.0;
   LGB_CUDA(cudaMemcpyAsync(w.unit2, &one, sizeof(double), cudaMemcpyHostToDevice, s));
   SplitMftProblem p{};
-  p.m = m; p.n = n; p.M = M; p.N = N; p.kp1 = kp1; p.kp2 = kp2; p.L = 1; p.batch = 1;
+  p.m = m; p.n = n; p.M = M; p.N = N; p.kp1 = kp1; p.kp2 = kp2; p.L = 1; p.batch = count;
   p.bf16 = bf16;
   p.e1_hi = w.e1h; p.e1_lo = w.e1l; p.f_hi = w.fh; p.f_lo = w.fl;
   p.e2_hi = w.e2h; p.e2_lo = w.e2l; p.g_hi = w.gh; p.g_lo = w.gl;
@@ -161,6 +172,14 @@ extern "C" int lgb_dft2(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int
   p.complex_scale = scale;
   p.err = w.err;
   return launch_split_mft(p, s);
+}
+
+extern "C" int lgb_dft2(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int N,
+                        double alpha_r, double alpha_c, double shift_r, double shift_c,
+                        double offset_r, double offset_c, int unitary, int precision,
+                        void* workspace, size_t workspace_bytes, lgb_stream stream) {
+  return lgb_dft2_batch(f, 1, m, n, F, M, N, alpha_r, alpha_c, shift_r, shift_c, offset_r,
+                        offset_c, unitary, precision, workspace, workspace_bytes, stream);
 }
 
 // Device status of the last dft2 that used this workspace (synchronises the

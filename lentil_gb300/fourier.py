@@ -102,6 +102,33 @@ def dft2(f, alpha, shape=None, shift=(0, 0), offset=(0, 0), unitary=True, out=No
     return _finish(F, out, host)
 
 
+def dft2_batch(f, alpha, shape=None, shift=(0, 0), offset=(0, 0), unitary=True, npix=None,
+               precision='fp64'):
+    """``dft2`` of every field of a stack ``f`` [count, m, n] with one
+    geometry (an extension of lentil's dft2, which takes one array): the DFT
+    matrices are built once and the split path transforms the whole stack in
+    one pair of tensor-core launches.  Returns [count, M, N], on the device
+    for CUDA input, else as numpy."""
+    host = not dv.is_tensor(f)
+    fd = dv.to_device(f, torch.complex128)
+    if fd.dim() != 3:
+        raise ValueError('dft2_batch expects a 3-D stack [count, m, n]')
+    count, m, n = (int(x) for x in fd.shape)
+    M, N = _shape(shape, npix, (m, n))
+    ar, ac = _pair(alpha, 'alpha')
+    sr, sc = _pair(shift, 'shift')
+    orow, ocol = _pair(offset, 'offset')
+    prec = _lib.precision_code(precision)
+    F = torch.empty((count, M, N), dtype=torch.complex128, device=fd.device)
+    nbytes = _lib.load().lgb_dft2_batch_workspace_size(count, m, n, M, N, prec)
+    ws = dv.workspace(nbytes)
+    _lib.call('lgb_dft2_batch', fd.data_ptr(), count, m, n, F.data_ptr(), M, N, ar, ac, sr, sc,
+              orow, ocol, int(bool(unitary)), prec, ws.data_ptr(), nbytes, dv.stream_ptr())
+    if prec != _lib.FP64:
+        _lib.call('lgb_dft2_status', ws.data_ptr(), dv.stream_ptr())
+    return dv.to_host(F) if host else F
+
+
 def idft2(F, alpha, shape=None, shift=(0, 0), unitary=True, out=None, npix=None,
           precision='fp64'):
     """Inverse DFT ``conj(dft2(conj(F))) / F.size`` (lentil/fourier.py:124-198)."""

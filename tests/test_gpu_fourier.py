@@ -128,3 +128,27 @@ def test_dft2_config_sizes(cuda_device, precision):
     # wavelengths of the broadband workload it averages to ~1.5e-7
     tol = {'fp64': 1e-12, 'split-bf16': 2e-6, 'split-fp16': 2e-6}[precision]
     assert e < tol, e
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split-bf16', 'split-fp16'])
+def test_dft2_batch_matches_single_and_oracle(cuda_device, precision):
+    # a stack of fields with one geometry: one batched transform equals the
+    # per-field transforms (and the oracle, within each path's tolerance)
+    rng = np.random.default_rng(21)
+    count, m, n = 3, 70, 53
+    f = rng.standard_normal((count, m, n)) + 1j * rng.standard_normal((count, m, n))
+    f[1] *= 1e-3                                   # fields with different scales
+    kw = dict(shape=(64, 81), shift=(0.4, -1.5), offset=(3, -2), unitary=True)
+    alpha = (0.011, 0.0093)
+    F = lg.fourier.dft2_batch(f, alpha, precision=precision, **kw)
+    assert isinstance(F, np.ndarray) and F.shape == (count, 64, 81)
+    tol = FP64_TOL if precision == 'fp64' else SPLIT_TOL[precision]     # random fields
+    for k in range(count):
+        ref = lo.dft2(f[k], alpha, **kw)
+        assert lo.peak_normalised_error(F[k], ref) < tol
+        single = lg.fourier.dft2(f[k], alpha, precision=precision, **kw)
+        assert lo.peak_normalised_error(F[k], single) < (1e-14 if precision == 'fp64' else 1e-12)
+    T = lg.fourier.dft2_batch(torch.as_tensor(f, device='cuda'), alpha, precision=precision, **kw)
+    assert isinstance(T, torch.Tensor) and T.is_cuda
+    with pytest.raises(ValueError):
+        lg.fourier.dft2_batch(f[0], alpha, precision=precision, **kw)
