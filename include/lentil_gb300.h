@@ -163,10 +163,15 @@ int lgb_pixel(const double* img, int rows, int cols, int oversample, double* out
 /* ------------------------------------------------------------------------
  * Pixelation.  Replaces lentil/detector.py:225-251 (pixelate = pixel, then
  * lentil/util.py:261-349 rescale(1/os, order=3, mode='nearest',
- * unitary=True)).  For N a multiple of os every resample point is a grid
- * point, so out (N/os x N/os) = p[::os, ::os] * sum(p)/sum(p[::os, ::os]),
- * zero where the sample is zero.  N % os != 0 -> LGB_EUNSUPPORTED.
+ * unitary=True)).  out is S x S with S = lgb_pixelate_size(N, os) =
+ * ceil(N * (1/os)) (lentil/util.py:323-324).  When every resample point is
+ * a grid point (N a multiple of os) out = p[::os, ::os] * sum(p)/sum(that),
+ * zero where the sample is zero; otherwise the cubic B-spline resampling
+ * of scipy.ndimage.map_coordinates(order=3, mode='nearest') folded into one
+ * banded FP64 operator per axis, out = G . p . G^T, then the same unitary
+ * scale and lentil's linearly interpolated nonzero mask (util.py:333-347).
  * ---------------------------------------------------------------------- */
+int lgb_pixelate_size(int N, int oversample);
 int lgb_pixelate(const double* img, int rows, int cols, int oversample, double* out,
                  void* workspace, size_t workspace_bytes, lgb_stream stream);
 

@@ -59,6 +59,7 @@ SIGNATURES = {
                                    c_void_p, c_int, c_int, c_void_p]),
     'lgb_pixel_workspace_size': (c_size_t, [c_int, c_int]),
     'lgb_pixel': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
+    'lgb_pixelate_size': (c_int, [c_int, c_int]),
     'lgb_pixelate': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t,
                              c_void_p]),
     'lgb_ptt_normal_workspace_size': (c_size_t, [c_int]),

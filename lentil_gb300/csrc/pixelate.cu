@@ -10,7 +10,8 @@
 // pixelate then resamples by 1/os with a cubic spline (lentil/util.py:261-349);
 // when N is a multiple of os every sample falls on a grid point, so the
 // result is d = p[::os, ::os] rescaled by sum(p)/sum(d) and masked where
-// d == 0 -- the only case implemented.
+// d == 0; otherwise the spline evaluation runs as two banded FP64 passes
+// (the off-grid section below).
 //
 // The same FFT machinery also filters white noise for lgb_power_spectrum
 // (lentil/wfe.py:8-70), defined at the end of this file.
@@ -215,6 +216,161 @@ __global__ void pixelate_scale_kernel(int count, const double* __restrict__ d,
   out[p] = (v != 0.0) ? v * (sums[0] / sums[1]) : 0.0;
 }
 
+// ------------------------------------------------- off-grid cubic resampling
+// lentil resamples with scipy.ndimage.map_coordinates(order=3,
+// mode='nearest') at x_k = (k - S/2) / (1/os) + N/2 on both axes
+// (lentil/util.py:323-340).  That evaluation is: pad the image by RS_PAD
+// edge copies per side, prefilter each axis of the padded image into cubic
+// B-spline coefficients with a half-sample-symmetric boundary, and sum the
+// four coefficients around x + RS_PAD weighted by the cubic B-spline
+// beta3 (Unser, Aldroubi & Eden, IEEE TSP 41(2), 1993).  The prefilter is
+// the symmetric convolution with h[t] = sqrt(3) z^|t|, z = sqrt(3) - 2, so
+// each output sample is a fixed linear combination of a window of input
+// samples: with h truncated at |t| <= RS_TAPS (|z|^31 < 2e-18 of the
+// signal) the window is RS_BW = 2 RS_TAPS + 4 wide, and the whole
+// resampling is out = G p G^T with G banded, S x RS_BW plus a start index
+// per row.  Both passes are FP64 FMA over L2-resident operands.
+constexpr int RS_PAD = 12, RS_TAPS = 30, RS_BW = 2 * RS_TAPS + 4;
+
+__host__ __device__ __forceinline__ double rs_coord(int k, int S, int N, int os) {
+  return ((double)k - S / 2.0) / (1.0 / os) + N / 2.0;
+}
+
+__device__ __forceinline__ int rs_reflect(int r, int L) {   // half-sample symmetric
+  r %= 2 * L;
+  if (r < 0) r += 2 * L;
+  return r >= L ? 2 * L - 1 - r : r;
+}
+
+__device__ __forceinline__ double rs_beta3(double t) {
+  t = fabs(t);
+  if (t < 1.0) return 2.0 / 3.0 - t * t + t * t * t / 2.0;
+  if (t < 2.0) { const double u = 2.0 - t; return u * u * u / 6.0; }
+  return 0.0;
+}
+
+__device__ __forceinline__ int rs_start(int k, int S, int N, int os) {
+  const int i0 = (int)floor(rs_coord(k, S, N, os) + RS_PAD) - 1;
+  return min(max(i0 - RS_TAPS - RS_PAD, 0), max(0, N - RS_BW));
+}
+
+// Gt[b][k] = weight of input sample q0[k] + b in output sample k
+__global__ void resample_operator_kernel(int N, int os, int S, double* __restrict__ Gt,
+                                         int* __restrict__ q0) {
+  __shared__ double h[RS_TAPS + 1];
+  if (threadIdx.x == 0) {
+    const double z = sqrt(3.0) - 2.0;
+    h[0] = sqrt(3.0);
+    for (int a = 1; a <= RS_TAPS; ++a) h[a] = h[a - 1] * z;
+  }
+  __syncthreads();
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= S * RS_BW) return;
+  const int k = idx / RS_BW, b = idx - k * RS_BW;
+  const int Np = N + 2 * RS_PAD;
+  const double xp = rs_coord(k, S, N, os) + RS_PAD;
+  const int i0 = (int)floor(xp) - 1;
+  const int start = rs_start(k, S, N, os);
+  const int want = start + b;
+  double g = 0.0;
+  for (int j = i0; j < i0 + 4; ++j) {
+    const double w = rs_beta3(xp - j);
+    const int jj = rs_reflect(j, Np);
+    for (int t = -RS_TAPS; t <= RS_TAPS; ++t) {
+      const int q = min(max(rs_reflect(jj - t, Np) - RS_PAD, 0), N - 1);
+      if (q == want) g += w * h[t < 0 ? -t : t];
+    }
+  }
+  Gt[(size_t)b * S + k] = g;
+  if (b == 0) q0[k] = start;
+}
+
+constexpr int RS_ROWS = 8;        // image rows per thread in the row pass
+
+// Tm[r][l] = sum_b Gt[b][l] p[r][q0[l] + b]; block (64, 4), RS_ROWS rows a thread
+__global__ void __launch_bounds__(256) resample_rows_kernel(const double* __restrict__ p, int N,
+                                                            int S, const double* __restrict__ Gt,
+                                                            const int* __restrict__ q0,
+                                                            double* __restrict__ Tm) {
+  const int l = blockIdx.x * 64 + threadIdx.x;
+  const int r0 = (blockIdx.y * 4 + threadIdx.y) * RS_ROWS;
+  if (l >= S || r0 >= N) return;
+  const int q = q0[l];
+  const int nb = min(RS_BW, N - q);
+  const int nr = min(RS_ROWS, N - r0);
+  const double* src = p + (size_t)r0 * N + q;
+  double acc[RS_ROWS];
+#pragma unroll
+  for (int i = 0; i < RS_ROWS; ++i) acc[i] = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    const double g = Gt[(size_t)b * S + l];
+#pragma unroll
+    for (int i = 0; i < RS_ROWS; ++i)
+      if (i < nr) acc[i] = fma(g, src[(size_t)i * N + b], acc[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < RS_ROWS; ++i)
+    if (i < nr) Tm[(size_t)(r0 + i) * S + l] = acc[i];
+}
+
+constexpr int RS_OUT = 4;         // output rows per thread in the column pass
+
+// raw[k][l] = sum_b Gt[b][k] Tm[q0[k] + b][l]; sums[2] += sum raw
+__global__ void __launch_bounds__(256) resample_cols_kernel(const double* __restrict__ Tm, int N,
+                                                            int S, const double* __restrict__ Gt,
+                                                            const int* __restrict__ q0,
+                                                            double* __restrict__ raw,
+                                                            double* __restrict__ sums) {
+  const int l = blockIdx.x * 64 + threadIdx.x;
+  const int k0 = (blockIdx.y * 4 + threadIdx.y) * RS_OUT;
+  double part = 0.0;
+  if (l < S) {
+    for (int i = 0; i < RS_OUT && k0 + i < S; ++i) {
+      const int k = k0 + i, q = q0[k];
+      const int nb = min(RS_BW, N - q);
+      const double* src = Tm + (size_t)q * S + l;
+      double acc = 0.0;
+      for (int b = 0; b < nb; ++b) acc = fma(Gt[(size_t)b * S + k], src[(size_t)b * S], acc);
+      raw[(size_t)k * S + l] = acc;
+      part += acc;
+    }
+  }
+  part = warp_sum(part);
+  if ((threadIdx.x & 31) == 0) atomicAdd(sums + 2, part);
+}
+
+// out = (raw * (sum p / sum raw)) * mask, the mask being the order-1
+// nearest-mode interpolation of (p != 0) at the same points, zeroed below
+// DBL_EPSILON (lentil/util.py:317-320, 333-347)
+__global__ void resample_finish_kernel(const double* __restrict__ raw,
+                                       const double* __restrict__ p, int N, int S, int os,
+                                       const double* __restrict__ sums, double* __restrict__ out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= S * S) return;
+  const int k = idx / S, l = idx - k * S;
+  const double y = rs_coord(k, S, N, os), x = rs_coord(l, S, N, os);
+  const int iy = (int)floor(y), ix = (int)floor(x);
+  const double fy = y - iy, fx = x - ix;
+  const int ya = min(max(iy, 0), N - 1), yb = min(max(iy + 1, 0), N - 1);
+  const int xa = min(max(ix, 0), N - 1), xb = min(max(ix + 1, 0), N - 1);
+  auto m = [&](int r, int c) { return p[(size_t)r * N + c] != 0.0 ? 1.0 : 0.0; };
+  double mask = (1.0 - fy) * ((1.0 - fx) * m(ya, xa) + fx * m(ya, xb)) +
+                fy * ((1.0 - fx) * m(yb, xa) + fx * m(yb, xb));
+  if (mask < 2.220446049250313e-16) mask = 0.0;
+  out[idx] = (raw[idx] * (sums[0] / sums[2])) * mask;
+}
+
+// S = ceil(N * (1/os)), evaluated as numpy does (lentil/util.py:323-324)
+static int resample_size(int N, int os) { return (int)std::ceil((double)N * (1.0 / os)); }
+
+// every resample point an exact grid point k * os
+static bool resample_on_grid(int N, int os, int S) {
+  if ((long long)S * os != N) return false;
+  for (int k = 0; k < S; ++k)
+    if (rs_coord(k, S, N, os) != (double)k * os) return false;
+  return true;
+}
+
 static bool fft_size(int N, int* logN) {
   if (N < 2 || N > 8192 || (N & (N - 1))) return false;
   int l = 0;
@@ -224,12 +380,15 @@ static bool fft_size(int N, int* logN) {
 }
 
 struct PixelSpace {
-  double* sums;
+  double* sums;          // [0] sum p, [1] sum of the grid samples, [2] sum of the resampled
   double* d;
   // GEMM path
   double *c, *C, *T, *P;
   // FFT path
   double2 *X, *Y, *tw;
+  // off-grid resampling: |.| of the MTF product (FFT path), operator, passes
+  double *Pabs, *Gt, *Tm, *raw;
+  int* q0;
 };
 
 static size_t pixel_space(void* ws, int N, int os, PixelSpace* s) {
@@ -246,7 +405,8 @@ static size_t pixel_space(void* ws, int N, int os, PixelSpace* s) {
   const int Nd = N / std::max(os, 1);
   t.sums = static_cast<double*>(take(4 * sizeof(double)));
   t.d = static_cast<double*>(take((size_t)Nd * Nd * sizeof(double)));
-  if (fft_size(N, &logN)) {
+  const bool fft = fft_size(N, &logN);
+  if (fft) {
     t.X = static_cast<double2*>(take(NN * sizeof(double2)));
     t.Y = static_cast<double2*>(take(NN * sizeof(double2)));
     t.tw = static_cast<double2*>(take((size_t)(N / 2) * sizeof(double2)));
@@ -255,6 +415,15 @@ static size_t pixel_space(void* ws, int N, int os, PixelSpace* s) {
     t.C = static_cast<double*>(take(NN * sizeof(double)));
     t.T = static_cast<double*>(take(NN * sizeof(double)));
     t.P = static_cast<double*>(take(NN * sizeof(double)));
+  }
+  const int S = resample_size(N, std::max(os, 1));
+  if (!resample_on_grid(N, std::max(os, 1), S)) {
+    // decided by the path, not by a pointer: the size query carves from null
+    if (fft) t.Pabs = static_cast<double*>(take(NN * sizeof(double)));
+    t.Gt = static_cast<double*>(take((size_t)RS_BW * S * sizeof(double)));
+    t.q0 = static_cast<int*>(take((size_t)S * sizeof(int)));
+    t.Tm = static_cast<double*>(take((size_t)N * S * sizeof(double)));
+    t.raw = static_cast<double*>(take((size_t)S * S * sizeof(double)));
   }
   if (s) *s = t;
   return off;
@@ -461,22 +630,36 @@ extern "C" int lgb_pixelate(const double* img, int rows, int cols, int oversampl
   LGB_REQUIRE(img && out && workspace, LGB_EINVAL, "pixelate: null pointer");
   LGB_REQUIRE(rows == cols, LGB_EINVAL, "pixelate: the pixel MTF is defined for square images");
   LGB_REQUIRE(rows > 0 && oversample > 0, LGB_EINVAL, "pixelate: sizes must be positive");
-  LGB_REQUIRE(rows % oversample == 0, LGB_EUNSUPPORTED,
-              "pixelate: the image size must be a multiple of oversample (the resampling "
-              "then falls on grid points)");
   LGB_REQUIRE(workspace_bytes >= lgb_pixel_workspace_size(rows, oversample), LGB_EWORKSPACE,
               "pixelate: workspace too small");
-  const int N = rows, os = oversample, Nd = N / os;
+  const int N = rows, os = oversample, S = resample_size(N, os);
   cudaStream_t s = as_stream(stream);
   PixelSpace w;
   const void* src;
   bool cplx;
   int st = run_pixel(img, N, os, workspace, s, &w, &src, &cplx);
   if (st) return st;
-  if ((st = abs_reduce(N, os, src, cplx, nullptr, w.d, w.sums, s))) return st;
-  pixelate_scale_kernel<<<cdiv(Nd * Nd, 256), 256, 0, s>>>(Nd * Nd, w.d, w.sums, out);
+  if (resample_on_grid(N, os, S)) {
+    if ((st = abs_reduce(N, os, src, cplx, nullptr, w.d, w.sums, s))) return st;
+    pixelate_scale_kernel<<<cdiv(S * S, 256), 256, 0, s>>>(S * S, w.d, w.sums, out);
+    LGB_CUDA(cudaGetLastError());
+    return LGB_OK;
+  }
+  double* P = cplx ? w.Pabs : w.P;
+  if ((st = abs_reduce(N, 1, src, cplx, P, nullptr, w.sums, s))) return st;
+  resample_operator_kernel<<<cdiv(S * RS_BW, 256), 256, 0, s>>>(N, os, S, w.Gt, w.q0);
+  resample_rows_kernel<<<dim3(cdiv(S, 64), cdiv(N, 4 * RS_ROWS)), dim3(64, 4), 0, s>>>(
+      P, N, S, w.Gt, w.q0, w.Tm);
+  resample_cols_kernel<<<dim3(cdiv(S, 64), cdiv(S, 4 * RS_OUT)), dim3(64, 4), 0, s>>>(
+      w.Tm, N, S, w.Gt, w.q0, w.raw, w.sums);
+  resample_finish_kernel<<<cdiv(S * S, 256), 256, 0, s>>>(w.raw, P, N, S, os, w.sums, out);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
+}
+
+extern "C" int lgb_pixelate_size(int N, int oversample) {
+  if (N <= 0 || oversample <= 0) return -1;
+  return resample_size(N, oversample);
 }
 
 extern "C" size_t lgb_power_spectrum_workspace_size(int N) {

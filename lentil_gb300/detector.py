@@ -27,9 +27,11 @@ def pixel(img, oversample=1):
 
 
 def pixelate(img, oversample):
-    """Pixel MTF, then resampling to native pixels (lentil/detector.py:225-251).
-    The image size must be a multiple of ``oversample``."""
+    """Pixel MTF, then cubic-spline resampling to native pixels
+    (lentil/detector.py:225-251, lentil/util.py:261-349): an
+    ceil(N / oversample)-square image."""
     os_ = int(oversample)
-    if os_ != oversample:
-        raise NotImplementedError('pixelate needs an integer oversample')
-    return _run('pixelate', img, os_, lambda n: (n // os_, n // os_))
+    if os_ != oversample or os_ < 1:
+        raise NotImplementedError('pixelate needs a positive integer oversample')
+    size = _lib.load().lgb_pixelate_size
+    return _run('pixelate', img, os_, lambda n: (size(int(n), os_),) * 2)

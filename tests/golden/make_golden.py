@@ -198,6 +198,16 @@ def main(ref_root):
         dd[f'{name}_os'] = np.asarray(os_)
         dd[f'{name}_pixel'] = lentil.detector.pixel(img, os_)
         dd[f'{name}_pixelate'] = lentil.detector.pixelate(img, os_)
+    # sizes that are not a multiple of oversample: off-grid spline resampling
+    # (own generator, so the cases above keep their inputs)
+    rng_off = np.random.default_rng(20261204)
+    for name, n, os_ in (('px100os3', 100, 3), ('px75os2', 75, 2), ('px61os7', 61, 7),
+                         ('px128os3', 128, 3), ('px64os5', 64, 5)):
+        img = rng_off.uniform(0, 1, (n, n)) ** 4
+        dd[f'{name}_img'] = img
+        dd[f'{name}_os'] = np.asarray(os_)
+        dd[f'{name}_pixel'] = lentil.detector.pixel(img, os_)
+        dd[f'{name}_pixelate'] = lentil.detector.pixelate(img, os_)
     np.savez_compressed(os.path.join(HERE, 'detector.npz'), **dd)
 
     # ---------------------------------------------------------- generators

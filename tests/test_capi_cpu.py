@@ -5,6 +5,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 from lentil_gb300 import _build, _lib
@@ -64,6 +65,21 @@ def test_workspace_sizes_are_consistent(lib):
     b = lib.lgb_dft2_workspace_size(100, 90, 128, 120, _lib.SPLIT_BF16)
     assert b > 0
     assert lib.lgb_idft2_workspace_size(100, 90, 128, 120, 0) >= a + 16 * 100 * 90
+
+
+@pytest.mark.parametrize('n,os_', [(2048, 3), (1000, 3), (64, 5), (75, 2), (5, 2)])
+def test_pixel_workspace_covers_off_grid_buffers(lib, n, os_):
+    # the size query must count every buffer the off-grid pixelate carves:
+    # the MTF product (two complex planes on the FFT path, three real
+    # planes on the GEMM path), |p| (FFT path), the banded operator, both
+    # resampling passes
+    S = lib.lgb_pixelate_size(n, os_)
+    assert S == int(np.ceil(n * (1 / os_)))
+    fft = n >= 2 and n & (n - 1) == 0
+    need = (2 * 16 + 8) * n * n if fft else 3 * 8 * n * n
+    need += 8 * (64 * S + n * S + S * S) + 4 * S
+    assert lib.lgb_pixel_workspace_size(n, os_) >= need
+    assert lib.lgb_pixelate_size(0, 2) == -1 and lib.lgb_pixelate_size(10, 0) == -1
 
 
 def test_build_is_up_to_date():

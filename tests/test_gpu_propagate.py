@@ -193,7 +193,8 @@ def test_plan_batch_matches_single(cuda_device):
             assert lo.peak_normalised_error(outb[b], o1[0]) < tol
 
 
-@pytest.mark.parametrize('name', ['px64os2', 'px90os3', 'px128os4'])
+@pytest.mark.parametrize('name', ['px64os2', 'px90os3', 'px128os4',          # grid samples
+                                  'px100os3', 'px75os2', 'px61os7', 'px128os3', 'px64os5'])
 def test_pixel_pixelate_golden(golden, cuda_device, name):
     # lentil/detector.py:167-251 against lentil's own outputs
     g = golden('detector')
@@ -207,10 +208,26 @@ def test_pixel_unitary_and_errors(cuda_device):
     a = np.random.default_rng(2).uniform(0, 1, (100, 100))
     assert np.isclose(np.sum(a), np.sum(lg.detector.pixel(a, oversample=1)), rtol=1e-12)
     assert lg.detector.pixelate(np.ones((10, 10)), 2).shape == (5, 5)
+    assert lg.detector.pixelate(np.ones((10, 10)), 3).shape == (4, 4)     # ceil(10/3)
     with pytest.raises(ValueError):
         lg.detector.pixel(np.ones((10, 12)), 2)
     with pytest.raises(NotImplementedError):
-        lg.detector.pixelate(np.ones((10, 10)), 3)
+        lg.detector.pixelate(np.ones((10, 10)), 2.5)
+
+
+@pytest.mark.parametrize('n,os_', [(5, 2), (33, 4), (200, 16), (1000, 3), (2048, 3)])
+def test_pixelate_off_grid_matches_oracle(cuda_device, n, os_):
+    # off-grid cubic resampling (N % os != 0; both pixel-MTF paths: FFT for
+    # 2048, circulant GEMMs otherwise) against the oracle; numpy in -> numpy
+    # out, CUDA tensor in -> CUDA tensor out
+    img = np.random.default_rng(n).uniform(0, 1, (n, n)) ** 4
+    ref = lo.pixelate(img, os_)
+    out = lg.detector.pixelate(img, os_)
+    assert isinstance(out, np.ndarray) and out.shape == ref.shape
+    assert lo.peak_normalised_error(out, ref) < 1e-12
+    assert np.isclose(out.sum(), ref.sum(), rtol=1e-12)
+    t = lg.detector.pixelate(torch.as_tensor(img, device='cuda'), os_)
+    assert t.is_cuda and lo.peak_normalised_error(t.cpu().numpy(), ref) < 1e-12
 
 
 @pytest.mark.parametrize('precision,tol', [('fp64', 1e-11), ('split-bf16', 3e-6)])

@@ -84,12 +84,34 @@ def test_field_merge_reduce_insert(golden):
     assert np.array_equal(out, g['insert_complex'])
 
 
-@pytest.mark.parametrize('name', ['px64os2', 'px90os3', 'px128os4'])
+PIXELATE_CASES = ['px64os2', 'px90os3', 'px128os4',                     # grid samples
+                  'px100os3', 'px75os2', 'px61os7', 'px128os3', 'px64os5']  # off grid
+
+
+@pytest.mark.parametrize('name', PIXELATE_CASES)
 def test_pixelate(golden, name):
     g = golden('detector')
     img, os_ = g[f'{name}_img'], int(g[f'{name}_os'])
     assert lo.peak_normalised_error(lo.pixel(img, os_), g[f'{name}_pixel']) < 1e-13
     assert lo.peak_normalised_error(lo.pixelate(img, os_), g[f'{name}_pixelate']) < 1e-12
+    # the banded-operator restatement the off-grid kernels follow
+    assert lo.peak_normalised_error(lo.pixelate_banded(img, os_), g[f'{name}_pixelate']) < 1e-13
+
+
+@pytest.mark.parametrize('n,os_', [(5, 2), (10, 3), (33, 4), (200, 16), (97, 3)])
+def test_resample_operator_matches_scipy(n, os_):
+    # G . s . G^T == map_coordinates(order=3, mode='nearest') at lentil's points,
+    # including sizes below the window width and large oversampling
+    from scipy.ndimage import map_coordinates
+    s = np.random.default_rng(n).uniform(0, 1, (n, n)) ** 3
+    S, x, q0, G = lo.resample_operator(n, os_)
+    nb = min(lo.RS_BW, n)
+    rows = np.stack([s[:, q0[l]:q0[l] + nb] @ G[l, :nb] for l in range(S)], axis=1)
+    out = np.stack([G[k, :nb] @ rows[q0[k]:q0[k] + nb, :] for k in range(S)], axis=0)
+    xx, yy = np.meshgrid(x, x)
+    ref = map_coordinates(s, [yy, xx], order=3, mode='nearest')
+    assert out.shape == (int(np.ceil(n * (1 / os_))),) * 2
+    assert lo.peak_normalised_error(out, ref) < 1e-14
 
 
 @pytest.mark.parametrize('name', FFT_CASES)
