@@ -53,6 +53,12 @@ def parse():
     ap.add_argument('--rates', default='10,50,200,1000',
                     help='serving: Poisson arrival rates (requests/s)')
     ap.add_argument('--duration', type=float, default=2.0, help='serving: seconds per rate')
+    ap.add_argument('--tile', type=int, default=0, choices=[0, 128, 256],
+                    help='tensor-core MFT pair-tile width: 0 = the autotuner\'s choice '
+                         '(measured per launch shape), 128 or 256 = forced')
+    ap.add_argument('--tune', default='measure', choices=['measure', 'model'],
+                    help='autotuner mode when --tile is 0: time both widths online per '
+                         'launch class, or take the occupancy model\'s choice')
     ap.add_argument('--workload', default='broadband',
                     choices=['broadband', 'monochromatic', 'phase_retrieval', 'serving', 'large'],
                     help='broadband: the headline workload; the others measure the '
@@ -415,7 +421,8 @@ def run_gpu(args):
         'data': 'synthetic (seeded)',
         'config': config_dict(wl, args, {'precision': args.precision,
                                          'field': [m, n], 'window': [M, N],
-                                         'parallelism': f'replicas x{world}'}),
+                                         'parallelism': f'replicas x{world}',
+                                         'mft_tile': tuner_summary(args)}),
         'p50_ms': statistics.median(step_ms), 'p99_ms': float(np.percentile(step_ms, 99)),
         'plan_build_ms': plan_ms,
         'err_vs_fp64': fp64_err,
@@ -482,6 +489,7 @@ def run_monochromatic(args):
     out = torch.empty((1,) + geo.shape_out, dtype=torch.float64, device='cuda')
     fused = lambda: plan.execute(A, O, W, out=out, check=False)
     f_mean, f_p50, f_p99 = _timed(fused, args.steps, args.warmup)
+    fused_tile = tuner_summary(args)
     ref_pl = lo.Pupil(amplitude=wl.amp, opd=opd, pixelscale=wl.pixelscale_in, focal_length=wl.focal_length)
     t0 = time.perf_counter()
     ref = lo.propagate_dft(lo.Wavefront(650e-9) * ref_pl, wl.det_pixelscale, shape=wl.det_shape,
@@ -510,7 +518,8 @@ def run_monochromatic(args):
             'p50_ms': f_p50, 'p99_ms': f_p99, 'higher_is_better': True,
             'dtype': args.precision, 'data': 'synthetic (seeded)',
             'config': {'workload': 'monochromatic 256^2 circular pupil, Noll 2-11 N(0,20nm), '
-                                   '650 nm, 128^2 detector x oversample 2'},
+                                   '650 nm, 128^2 detector x oversample 2',
+                       'mft_tile': fused_tile},
             'api_fp64': {'value': 1e3 / api_mean, 'p50_ms': api_p50, 'p99_ms': api_p99,
                          'err_vs_oracle': e_api},
             'err_vs_oracle': e_fused,
@@ -571,7 +580,7 @@ def run_phase_retrieval(args):
             'higher_is_better': True, 'dtype': args.precision, 'data': 'synthetic (seeded)',
             'config': {'workload': '512^2 circular pupil, Noll 2-37 + 18-segment PTT, 3 diversity '
                                    'images at -1/0/+1 wave defocus, 633 nm, 256^2 detector x2',
-                       'parameters': int(len(sigma))},
+                       'parameters': int(len(sigma)), 'mft_tile': tuner_summary(args)},
             'mft_tflops_algorithmic': flops / (mean / 1e3) / 1e12}
     print(json.dumps(line), flush=True)
 
@@ -642,7 +651,8 @@ def run_serving(args):
                                    '64-1024 x oversample 2, 1-128 wavelengths on a 128-point '
                                    '400-1000 nm grid, circular '
                                    'or 18-hex amplitude, Noll 2-11 N(0,20nm)',
-                       'streams': 4, 'max_batch': 4, 'duration_s_per_rate': args.duration}}
+                       'streams': 4, 'max_batch': 4, 'duration_s_per_rate': args.duration,
+                       'mft_tile': tuner_summary(args)}}
     print(json.dumps(line), flush=True)
 
 
@@ -717,8 +727,21 @@ def run_large(args):
     print(json.dumps(line), flush=True)
 
 
+def tuner_summary(args):
+    """Tile width of this thread's last tensor-core launch and how it was chosen."""
+    from lentil_gb300 import tuner
+    how = {'measure': 'autotuner (online measurement)', 'model': 'autotuner (occupancy model)'}
+    return {'last_tile': tuner.last_tile(), 'classes_decided': tuner.entries(),
+            'chosen_by': f'forced --tile {args.tile}' if args.tile else how[args.tune]}
+
+
 def main():
     args = parse()
+    if args.impl != 'reference':
+        from lentil_gb300 import tuner
+        tuner.set_mode(args.tune)
+        if args.tile:
+            tuner.force_tile(args.tile)
     if args.workload == 'large':
         return run_large(args)
     if args.workload == 'serving':

@@ -320,10 +320,45 @@ int lgb_psf_plan_status(lgb_psf_plan plan, lgb_stream stream);
 #define LGB_PROFILE_OTHER 3
 #define LGB_PROFILE_SLOTS 4
 int lgb_psf_plan_profile(lgb_psf_plan plan, int enable);
+/* Pair-tile width of the plan's split launches: 0 (default) = the
+ * autotuner's choice (lgb_tuner_*), 256 or 128 = that width.  A caller that
+ * runs several executes at once (a server with launches in flight on other
+ * streams) sets 256, the width with the best MMA throughput per SM, since
+ * the narrower tile only pays when pairs would otherwise idle.  Read when an
+ * execute is issued. */
+int lgb_psf_plan_set_tile(lgb_psf_plan plan, int tile);
 int lgb_psf_plan_kernel_times(lgb_psf_plan plan, double* ms, int* launches, int n);
 /* Releases the plan's memory (stream-ordered on the creation stream); call
  * it after the plan's last execute has completed. */
 int lgb_psf_plan_destroy(lgb_psf_plan plan);
+
+/* ------------------------------------------------------------------------
+ * Tile-shape autotuner of the split-precision MFT (extension: lentil has no
+ * GPU path).  Every split launch (lgb_dft2/_batch/idft2 and plan executes)
+ * runs its CTA-pair tiles 256 or 128 output columns wide.  The width is
+ * chosen per launch class -- precision, m, n, M, N, epilogue and the
+ * occupancy of the problem count (waves of 128-wide tiles per stage over the
+ * resident CTA pairs, capped at 8) -- and cached for the process:
+ *   LGB_TUNE_MEASURE (default): tuned online on the caller's own launches.
+ *     The first launch of a class runs the occupancy model's width, the
+ *     second the other width, each bracketed by CUDA events on its stream;
+ *     a later launch that finds both finished (cudaEventQuery, no host wait)
+ *     caches the faster.  Nothing is relaunched or synchronised.  Launches
+ *     under stream capture use the cached or model width and time nothing.
+ *   LGB_TUNE_MODEL: the occupancy model decides at once.
+ * lgb_tuner_force_tile(256 | 128) makes every launch use that width (0: off).
+ * lgb_tuner_entries counts decided classes; lgb_tuner_lookup returns the
+ * decided width of the class of (m, n, M, N, count = PSFs x wavelengths,
+ * precision, epilogue 0 = intensity / 1 = complex field) or 0;
+ * lgb_tuner_last_tile the width of this thread's last split launch. */
+#define LGB_TUNE_MODEL 0
+#define LGB_TUNE_MEASURE 1
+int lgb_tuner_set_mode(int mode);
+int lgb_tuner_force_tile(int tile);
+void lgb_tuner_clear(void);
+int lgb_tuner_entries(void);
+int lgb_tuner_lookup(int m, int n, int M, int N, int count, int precision, int epilogue);
+int lgb_tuner_last_tile(void);
 
 #ifdef __cplusplus
 }

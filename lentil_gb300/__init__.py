@@ -4,10 +4,11 @@ Drop-in API of the path (same names and arguments as lentil 0.8.8):
 ``fourier.dft2``/``idft2``, ``propagate_dft``, ``propagate_fft``, ``Wavefront``, ``Plane``,
 ``Pupil``, ``Image``, ``Tilt``, ``field`` helpers and ``detector.pixelate``,
 plus the fused ``broadband_psf``/``PSFPlan``.  Every transform, phasor,
-overlap-add and pixelation runs in the library's own CUDA kernels
-(``liblentil_gb300.so``, C ABI in ``include/lentil_gb300.h``); there is no
-CPU fallback.  The aperture/OPD generators are host-side numpy helpers for
-building inputs, as in lentil.
+overlap-add, tilt fit, pixelation and Zernike/power-spectrum generation runs
+in the library's own CUDA kernels (``liblentil_gb300.so``, C ABI in
+``include/lentil_gb300.h``); there is no CPU fallback.  The aperture shapes
+are host-side numpy helpers for building inputs, as in lentil.
+``tuner`` controls the tile-shape autotuner of the tensor-core MFT.
 """
 __version__ = '0.1.0'
 
@@ -25,3 +26,4 @@ from .util import boundary, centroid, normalize_power, pad
 from .zernike import zernike, zernike_compose, zernike_basis, zernike_coordinates
 from .wfe import power_spectrum
 from . import _lib
+from . import tuner

@@ -60,6 +60,13 @@ SIGNATURES = {
     'lgb_pixel_workspace_size': (c_size_t, [c_int, c_int]),
     'lgb_pixel': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
     'lgb_pixelate_size': (c_int, [c_int, c_int]),
+    'lgb_psf_plan_set_tile': (c_int, [c_void_p, c_int]),
+    'lgb_tuner_set_mode': (c_int, [c_int]),
+    'lgb_tuner_force_tile': (c_int, [c_int]),
+    'lgb_tuner_clear': (None, []),
+    'lgb_tuner_entries': (c_int, []),
+    'lgb_tuner_lookup': (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_int]),
+    'lgb_tuner_last_tile': (c_int, []),
     'lgb_pixelate': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t,
                              c_void_p]),
     'lgb_ptt_normal_workspace_size': (c_size_t, [c_int]),

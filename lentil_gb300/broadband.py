@@ -100,6 +100,11 @@ class PSFPlan:
                 pass
             self._h = None
 
+    def set_tile(self, tile):
+        """Pair-tile width of this plan's tensor-core launches: 0 = the
+        autotuner's choice (``lentil_gb300.tuner``), 256 or 128 = that width."""
+        _lib.call('lgb_psf_plan_set_tile', self._h, int(tile))
+
     def workspace_bytes(self, count, n_sel=None):
         """Bytes of a caller workspace for ``execute(..., workspace=...)``."""
         return _lib.load().lgb_psf_execute_workspace_size(self._h, count,

@@ -91,6 +91,7 @@ struct SplitMftProblem {
   cudaEvent_t* events;     // optional [4]: recorded around the stage-1 and stage-2 launches
   const int* lam_idx;      // optional [L] device: wavelength -> DFT-matrix slot
   int L_bank;              // DFT-matrix slots held (when lam_idx is set)
+  int tile;                // pair-tile width 256 or 128; 0: the autotuner's choice
 };
 int launch_split_mft(const SplitMftProblem& p, cudaStream_t s);
 // scale applied to the stage-1 result before its 16-bit split

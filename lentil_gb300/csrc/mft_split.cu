@@ -48,6 +48,8 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <mutex>
 
 #include "common.cuh"
@@ -57,20 +59,34 @@ namespace lgb {
 namespace tc {
 
 constexpr int BM = 128;                                    // A rows per CTA (256 per pair)
-constexpr int BN = 256;                                    // output columns per pair tile
-constexpr int BNC = BN / 2;                                // B rows held per CTA
-constexpr int BK = 64, STAGES = 3;
+constexpr int BK = 64;
 constexpr int KSTEPS = BK / 16;                            // MMA k-steps per K block
 constexpr uint32_t A_BYTES = BM * BK * 2;                  // 16 KB per plane
-constexpr uint32_t B_BYTES = BNC * BK * 2;                 // 16 KB per plane
-constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 64 KB per CTA
 constexpr uint32_t BAR_BYTES = 128;
-constexpr uint32_t SMEM_BYTES = STAGES * STAGE_BYTES + 8 * 4096 + BAR_BYTES + 1024;
 constexpr int EPI_WARPS = 8;
 constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
-constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t ACC_COLS = 256;                         // one accumulator: 128 lanes x 256 fp32
+constexpr uint32_t STG_BYTES = 4096;                       // output staging per epilogue warp
 constexpr unsigned long long WAIT_NS = 2000000000ull;      // 2 s bound on any wait
+
+// Pair-tile width: 256 output columns (the fast shape for large transforms:
+// each A tile feeds twice the MMA work) or 128 (twice the tiles, for launches
+// too small to fill every CTA pair).  The autotuner at the end of this file
+// picks one per launch shape.  Both use the same 192 KB operand ring.
+template <int BN_>
+struct TileCfg {
+  static constexpr int BN = BN_;                           // output columns per pair tile
+  static constexpr int BNC = BN / 2;                       // B rows held per CTA
+  static constexpr int STAGES = BN == 256 ? 3 : 4;
+  static constexpr uint32_t B_BYTES = BNC * BK * 2;        // 16 / 8 KB per plane
+  static constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 64 / 48 KB per CTA
+  static constexpr uint32_t ACC_COLS = BN;                 // one accumulator: 128 lanes x BN fp32
+  static constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;      // double-buffered
+  static constexpr int RUN = BN / 2;                       // accumulator columns per epilogue warp
+  static constexpr uint32_t SMEM_BYTES =
+      STAGES * STAGE_BYTES + EPI_WARPS * STG_BYTES + BAR_BYTES + 1024;
+};
+static_assert(TileCfg<256>::SMEM_BYTES <= 232448 && TileCfg<128>::SMEM_BYTES <= 232448,
+              "shared memory per CTA");
 
 struct Params {
   int stage;                 // 1 or 2
@@ -97,9 +113,10 @@ struct Params {
   const int* lam_idx;        // [L] wavelength -> DFT-matrix slot, or null (identity)
 };
 
-// MMA N of column tile tn: 256, except a narrower last tile when the
+// MMA N of column tile tn: BN, except a narrower last tile when the
 // operand's columns end inside it (no MMA work on padding columns).  The
 // pair splits a tile's B rows evenly: CTA r holds rows r*N/2 .. of it.
+template <int BN>
 __device__ __forceinline__ int tile_n(const Params& p, int tn) {
   return tn == p.n_tiles - 1 ? p.n_last : BN;
 }
@@ -297,14 +314,21 @@ __device__ __forceinline__ Item decode(const Params& p, int i) {
 }
 
 // ------------------------------------------------------------- epilogue ---
-// Drain 128 columns of a TMEM region into the running sums (round to nearest).
-// One 32-column load in flight keeps the epilogue within the 168 registers
-// a thread gets when three warps share an SM sub-partition.
-__device__ __forceinline__ void drain_add(uint32_t taddr, float (&run)[128]) {
+// Drain this warp's RUN accumulator columns into the running sums (round to
+// nearest).  Columns: ch*RUN.. of the tile, except for 128-wide stage-2
+// tiles, whose real parts (the even CTA's B rows) fill columns 0..63 and
+// imaginary parts 64..127: there warp half ch takes real columns ch*32..
+// and the matching imaginary columns 64 + ch*32.., so that each thread holds
+// whole complex values.  One 32-column load in flight keeps the epilogue
+// within the 168 registers a thread gets when three warps share an SM
+// sub-partition.
+template <int RUN>
+__device__ __forceinline__ void drain_add(uint32_t trow, int stage, int ch, float (&run)[RUN]) {
 #pragma unroll
-  for (int h = 0; h < 4; ++h) {
+  for (int h = 0; h < RUN / 32; ++h) {
+    const int col = (RUN == 64 && stage == 2) ? h * 64 + ch * 32 : ch * RUN + h * 32;
     uint32_t a[32];
-    tmem_ld32(taddr + h * 32, a);
+    tmem_ld32(trow + col, a);
     tmem_ld_wait();
 #pragma unroll
     for (int j = 0; j < 32; ++j) run[h * 32 + j] += __uint_as_float(a[j]);
@@ -320,22 +344,20 @@ __device__ __forceinline__ void drain_add(uint32_t taddr, float (&run)[128]) {
 // asynchronously; the warp returns to draining the next item and waits for
 // the TMA to have read the slice only before it rewrites it.  TMA clips the
 // rows past M and the columns past the tensor's extent.
-constexpr uint32_t STG_BYTES = 4096;                       // per epilogue warp
-
 // Stage 1: G rows (split into hi/lo planes) = the stage-2 A operand, as two
 // 32 x 32 boxes (64-byte rows, 64-byte swizzle) per pass.  A warp's 32 rows
 // are 32 consecutive complex rows u with one plane half h.
-template <bool BF16>
+template <bool BF16, int BN, int RUN>
 __device__ __forceinline__ void write_stage1(const Params& p, const Item& w, int row, int ch,
-                                             const float (&run)[128], uint8_t* stg,
+                                             const float (&run)[RUN], uint8_t* stg,
                                              const CUtensorMap* map_hi, const CUtensorMap* map_lo) {
   const int lane = row & 31;
   const int h = row >> 6;
   const int u0 = w.tm * 64 + (row & 63) - lane;            // first row of this warp
-  const int c0 = w.tn * BN + ch * 128;
+  const int c0 = w.tn * BN + ch * RUN;
   const uint32_t s_hi = smem_u32(stg), s_lo = s_hi + 2048;
 #pragma unroll
-  for (int cc = 0; cc < 4; ++cc) {
+  for (int cc = 0; cc < RUN / 32; ++cc) {
     if (c0 + cc * 32 >= p.kp_out) break;                   // uniform over the warp
     if (lane == 0) bulk_wait_read();                       // previous box read out of the slice
     __syncwarp();
@@ -366,24 +388,26 @@ __device__ __forceinline__ void write_stage1(const Params& p, const Item& w, int
   }
 }
 
-// Stage 2 column layout of a 256-column tile: half ch holds output columns
-// v = tn*128 + ch*64 + j, real parts in [0, 64), imaginary in [64, 128).
-// Intensity: two 32 x 32 FP32 boxes (128-byte rows, 128-byte swizzle)
-// reduce-added into the window.
+// Stage 2: a warp holds HALF = RUN/2 complex output columns
+// v = tn*(BN/2) + ch*HALF + j, real parts in run[0, HALF), imaginary in
+// run[HALF, RUN).  Intensity: 32 x 32 FP32 boxes (128-byte rows, 128-byte
+// swizzle) reduce-added into the window.
+template <int BN, int RUN>
 __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int row, int ch,
-                                             const float (&run)[128], uint8_t* stg,
+                                             const float (&run)[RUN], uint8_t* stg,
                                              const CUtensorMap* map_w) {
+  constexpr int HALF = RUN / 2;
   const int lane = row & 31;
   const int u = w.tm * BM + row, u0 = u - lane;
   const float sf = pow2_scale_for(p.maxabs[w.psf]);
-  const int v0 = w.tn * 128 + ch * 64;
+  const int v0 = w.tn * (BN / 2) + ch * HALF;
   if (p.epilogue == 0) {
     const float inv = 1.f / (sf * p.sG);
     const double wt = p.weights ? p.weights[(size_t)w.psf * p.L + w.lam] : 1.0;
     const float coef = (float)(wt * p.unit2[matrix_slot(p, w.lam)]) * inv * inv;
     const uint32_t s0 = smem_u32(stg);
 #pragma unroll
-    for (int cc = 0; cc < 2; ++cc) {
+    for (int cc = 0; cc < HALF / 32; ++cc) {
       if (v0 + cc * 32 >= p.N) break;                      // uniform over the warp
       if (lane == 0) bulk_wait_read();
       __syncwarp();
@@ -393,7 +417,7 @@ __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const int j = cc * 32 + c * 4 + e;
-          r4[e] = coef * fmaf(run[j], run[j], run[64 + j] * run[64 + j]);
+          r4[e] = coef * fmaf(run[j], run[j], run[HALF + j] * run[HALF + j]);
         }
         *reinterpret_cast<float4*>(stg + lane * 128 + ((c ^ (lane & 7)) << 4)) =
             make_float4(r4[0], r4[1], r4[2], r4[3]);
@@ -410,18 +434,21 @@ __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int
     const double scl = p.cscale / ((double)sf * (double)p.sG);
     double2* outc = reinterpret_cast<double2*>(p.out) + ((size_t)w.q * p.M + u) * p.N;
 #pragma unroll
-    for (int j = 0; j < 64; ++j)
-      if (v0 + j < p.N) outc[v0 + j] = make_double2(scl * run[j], scl * run[64 + j]);
+    for (int j = 0; j < HALF; ++j)
+      if (v0 + j < p.N) outc[v0 + j] = make_double2(scl * run[j], scl * run[HALF + j]);
   }
 }
 
 // -------------------------------------------------------------- kernel ---
-template <bool BF16>
+template <bool BF16, int BN>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
                  const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo,
                  const __grid_constant__ CUtensorMap tmC0, const __grid_constant__ CUtensorMap tmC1,
                  const Params p) {
+  using C = TileCfg<BN>;
+  constexpr int STAGES = C::STAGES;
+  constexpr uint32_t STAGE_BYTES = C::STAGE_BYTES, B_BYTES = C::B_BYTES, ACC_COLS = C::ACC_COLS;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;
@@ -454,7 +481,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS));
+                 "r"(C::TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
   }
   tc_fence_before();
@@ -476,7 +503,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
         const int az = p.stage == 1 ? matrix_slot(p, w.lam) : w.q;
         const int bz = p.stage == 1 ? w.q : matrix_slot(p, w.lam);
         const int ay = (2 * w.tm + (int)rank) * BM;
-        const int by = w.tn * BN + (int)rank * (tile_n(p, w.tn) >> 1);
+        const int by = w.tn * BN + (int)rank * (tile_n<BN>(p, w.tn) >> 1);
         for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
           const int s = it % STAGES;
           if (!mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1, p.err)) { ok = false; break; }
@@ -502,7 +529,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
       bool ok = true;
       for (int i = pair; ok && i < p.n_items; i += npairs) {
         const uint32_t idesc = (p.idesc & ~(0x3Fu << 17)) |
-                               ((uint32_t)(tile_n(p, decode(p, i).tn) >> 3) << 17);
+                               ((uint32_t)(tile_n<BN>(p, decode(p, i).tn) >> 3) << 17);
         for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
           const int s = it % STAGES, xb = it & 1;
           if (!mbar_wait(full_bar(s), (it / STAGES) & 1, p.err)) { ok = false; break; }
@@ -533,7 +560,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
     const int q4 = warp & 3;                 // TMEM lane quadrant of this warp
     const int ch = (warp - 2) >> 2;          // column half of the tile
     const int row = q4 * 32 + lane;
-    const uint32_t trow = tmem + ((uint32_t)(q4 * 32) << 16) + ch * 128;
+    const uint32_t trow = tmem + ((uint32_t)(q4 * 32) << 16);
     const uint32_t empty_lead[2] = {map_to_cta(acc_empty(0), 0), map_to_cta(acc_empty(1), 0)};
     uint8_t* const stg = gbase + STAGES * STAGE_BYTES + (warp - 2) * STG_BYTES;
     uint32_t it = 0;
@@ -541,22 +568,22 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
     for (int i = pair; ok && i < p.n_items; i += npairs) {
       Item w = decode(p, i);
       w.tm = 2 * w.tm + (int)rank;           // this CTA's 128-row tile
-      float run[128];
+      float run[C::RUN];
 #pragma unroll
-      for (int j = 0; j < 128; ++j) run[j] = 0.f;
+      for (int j = 0; j < C::RUN; ++j) run[j] = 0.f;
       for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
         const int xb = it & 1;
         ok = __all_sync(0xffffffffu, mbar_wait(acc_full(xb), (it >> 1) & 1, p.err));
         if (!ok) break;
         tc_fence_after();
-        drain_add(trow + xb * ACC_COLS, run);
+        drain_add<C::RUN>(trow + xb * ACC_COLS, p.stage, ch, run);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive_cluster(empty_lead[xb]);
       }
       if (!ok) break;
-      if (p.stage == 1) write_stage1<BF16>(p, w, row, ch, run, stg, &tmC0, &tmC1);
-      else write_stage2(p, w, row, ch, run, stg, &tmC0);
+      if (p.stage == 1) write_stage1<BF16, BN, C::RUN>(p, w, row, ch, run, stg, &tmC0, &tmC1);
+      else write_stage2<BN, C::RUN>(p, w, row, ch, run, stg, &tmC0);
     }
     // the bulk stores / reduce-adds this warp issued have landed
     if (lane == 0) bulk_wait_all();
@@ -567,7 +594,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
   cluster_sync();                        // no CTA leaves while its pair may still use it
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TMEM_COLS));
   }
 }
 
@@ -618,43 +645,15 @@ static int make_map(CUtensorMap* map, const void* ptr, bool bf16, int K, int row
                       CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
-constexpr uint32_t make_idesc(bool bf16) {
+constexpr uint32_t make_idesc(bool bf16, int bn) {
   return (1u << 4)                          // D format: FP32
          | ((bf16 ? 1u : 0u) << 7)          // A format: BF16 (1) / FP16 (0)
          | ((bf16 ? 1u : 0u) << 10)         // B format
-         | ((uint32_t)(BN >> 3) << 17)      // N = 256
+         | ((uint32_t)(bn >> 3) << 17)      // N = tile width (narrower last tile per item)
          | ((uint32_t)((2 * BM) >> 4) << 24);  // M = 256 (the CTA pair)
 }
 
-// Largest number of CTA pairs of this kernel resident at once (per device).
-template <bool BF16>
-static int max_pairs(cudaLaunchConfig_t& cfg) {
-  static std::mutex mu;
-  static int cached[64] = {0};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  std::lock_guard<std::mutex> lock(mu);
-  if (cached[dev] == 0) {
-    int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, split_mft_kernel<BF16>, &cfg) != cudaSuccess) n = 0;
-    cached[dev] = n;
-  }
-  return cached[dev];
-}
-
-template <bool BF16>
-static int launch_one(const Params& p, const CUtensorMap& a_hi, const CUtensorMap& a_lo,
-                      const CUtensorMap& b_hi, const CUtensorMap& b_lo, const CUtensorMap& c0,
-                      const CUtensorMap& c1, cudaStream_t s) {
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
-  std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(split_mft_kernel<BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)SMEM_BYTES);
-  });
-  LGB_CUDA(attr_err);
-  if (p.n_items <= 0) return LGB_OK;
-  cudaLaunchAttribute attr[1];
+static cudaLaunchConfig_t pair_config(uint32_t smem, cudaStream_t s, cudaLaunchAttribute* attr) {
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = 2;
   attr[0].val.clusterDim.y = 1;
@@ -662,14 +661,306 @@ static int launch_one(const Params& p, const CUtensorMap& a_hi, const CUtensorMa
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2);
   cfg.blockDim = dim3(NUM_THREADS);
-  cfg.dynamicSmemBytes = SMEM_BYTES;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const int pairs = max_pairs<BF16>(cfg);
+  return cfg;
+}
+
+template <bool BF16, int BN>
+static cudaError_t set_smem_attr() {
+  static std::once_flag once;
+  static cudaError_t err = cudaSuccess;
+  std::call_once(once, [] {
+    err = cudaFuncSetAttribute(split_mft_kernel<BF16, BN>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)TileCfg<BN>::SMEM_BYTES);
+  });
+  return err;
+}
+
+// Largest number of CTA pairs of this kernel resident at once (per device).
+template <bool BF16, int BN>
+static int max_pairs() {
+  static std::mutex mu;
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (set_smem_attr<BF16, BN>() != cudaSuccess) return 0;
+  std::lock_guard<std::mutex> lock(mu);
+  if (cached[dev] == 0) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = pair_config(TileCfg<BN>::SMEM_BYTES, 0, attr);
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, split_mft_kernel<BF16, BN>, &cfg) != cudaSuccess) n = 0;
+    cached[dev] = n;
+  }
+  return cached[dev];
+}
+
+template <bool BF16, int BN>
+static int launch_one(const Params& p, const CUtensorMap& a_hi, const CUtensorMap& a_lo,
+                      const CUtensorMap& b_hi, const CUtensorMap& b_lo, const CUtensorMap& c0,
+                      const CUtensorMap& c1, cudaStream_t s) {
+  LGB_CUDA((set_smem_attr<BF16, BN>()));
+  if (p.n_items <= 0) return LGB_OK;
+  const int pairs = max_pairs<BF16, BN>();
   LGB_REQUIRE(pairs > 0, LGB_ECUDA, "split mft: no CTA pair of the tensor-core kernel fits on this GPU");
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = pair_config(TileCfg<BN>::SMEM_BYTES, s, attr);
   cfg.gridDim = dim3(2 * std::min(p.n_items, pairs));
-  LGB_CUDA(cudaLaunchKernelEx(&cfg, split_mft_kernel<BF16>, a_hi, a_lo, b_hi, b_lo, c0, c1, p));
+  LGB_CUDA(cudaLaunchKernelEx(&cfg, split_mft_kernel<BF16, BN>, a_hi, a_lo, b_hi, b_lo, c0, c1, p));
+  return LGB_OK;
+}
+
+template <int BN>
+static int launch_stage(const Params& p, bool bf16, const CUtensorMap* m, cudaStream_t s) {
+  return bf16 ? launch_one<true, BN>(p, m[0], m[1], m[2], m[3], m[4], m[5], s)
+              : launch_one<false, BN>(p, m[0], m[1], m[2], m[3], m[4], m[5], s);
+}
+
+// Work items and K blocks of each stage at tile width bn.
+struct StageShape {
+  long long items;
+  int kblocks;
+};
+static void stage_shapes(const SplitMftProblem& q, int bn, StageShape (&st)[2]) {
+  const long long Q = (long long)q.batch * q.L;
+  st[0].items = Q * cdiv(cdiv(q.M, 64), 2) * cdiv(q.kp2, bn);
+  st[0].kblocks = 2 * q.kp1 / BK;
+  st[1].items = Q * cdiv(q.M, 2 * BM) * cdiv(q.N, bn / 2);
+  st[1].kblocks = 2 * q.kp2 / BK;
+}
+
+// Both stages with pair tiles BN wide; ev (optional [4]) brackets the two
+// launches.  Every tensor map is encoded before the first launch, so the
+// host leaves no gap between the stages on the stream.
+template <int BN>
+static int run_split_mft(const SplitMftProblem& q, cudaEvent_t* ev, cudaStream_t s) {
+  using C = TileCfg<BN>;
+  const int Q = q.batch * q.L;
+  const int mrows1 = cdiv(q.M, 64) * 128;      // E1 block rows
+  const int nrows2 = cdiv(q.N, 128) * 256;     // E2 block rows
+  const int Lm = q.lam_idx ? q.L_bank : q.L;   // DFT-matrix slots held
+  CUtensorMap m1[6], m2[6];                    // a_hi, a_lo, b_hi, b_lo, c0, c1 per stage
+  StageShape sh[2];
+  stage_shapes(q, BN, sh);
+  int st;
+  // stage 1: G = E1 . f
+  if ((st = make_map(&m1[0], q.e1_hi, q.bf16, 2 * q.kp1, mrows1, Lm, BM))) return st;
+  if ((st = make_map(&m1[1], q.e1_lo, q.bf16, 2 * q.kp1, mrows1, Lm, BM))) return st;
+  if ((st = make_map(&m1[2], q.f_hi, q.bf16, 2 * q.kp1, q.n, Q, C::BNC))) return st;
+  if ((st = make_map(&m1[3], q.f_lo, q.bf16, 2 * q.kp1, q.n, Q, C::BNC))) return st;
+  if ((st = make_map_any(&m1[4], q.g_hi, half_type(q.bf16), 2, 2 * q.kp2, q.M, Q, 32, 32,
+                         CU_TENSOR_MAP_SWIZZLE_64B)))
+    return st;
+  if ((st = make_map_any(&m1[5], q.g_lo, half_type(q.bf16), 2, 2 * q.kp2, q.M, Q, 32, 32,
+                         CU_TENSOR_MAP_SWIZZLE_64B)))
+    return st;
+  // stage 2: F = G . E2 (+ epilogue)
+  if ((st = make_map(&m2[0], q.g_hi, q.bf16, 2 * q.kp2, q.M, Q, BM))) return st;
+  if ((st = make_map(&m2[1], q.g_lo, q.bf16, 2 * q.kp2, q.M, Q, BM))) return st;
+  if ((st = make_map(&m2[2], q.e2_hi, q.bf16, 2 * q.kp2, nrows2, Lm, C::BNC))) return st;
+  if ((st = make_map(&m2[3], q.e2_lo, q.bf16, 2 * q.kp2, nrows2, Lm, C::BNC))) return st;
+  m2[4] = m1[4];
+  m2[5] = m1[5];
+  if (q.epilogue == 0) {
+    LGB_REQUIRE(q.ldw % 4 == 0, LGB_EINVAL, "split mft: intensity window pitch must be a multiple of 4");
+    if ((st = make_map_any(&m2[4], q.wbuf, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, q.ldw, q.M, q.batch,
+                           32, 32, CU_TENSOR_MAP_SWIZZLE_128B)))
+      return st;
+  }
+
+  Params p{};
+  p.stage = 1;
+  p.kblocks = sh[0].kblocks;
+  p.m_tiles = cdiv(cdiv(q.M, 64), 2);          // pairs of 64-row (128 block-row) E1 tiles
+  p.n_tiles = cdiv(q.kp2, BN);
+  p.n_items = (int)sh[0].items;
+  p.L = q.L;
+  p.idesc = make_idesc(q.bf16, BN);
+  p.M = q.M; p.N = q.N;
+  p.kp_out = q.kp2;
+  p.n_last = q.kp2 - (p.n_tiles - 1) * BN;              // kp2 % 32 == 0, so n_last % 32 == 0
+  p.sG = split_g_scale(q.m);
+  p.g_hi = q.g_hi; p.g_lo = q.g_lo;
+  p.maxabs = q.maxabs;
+  p.err = q.err;
+  p.lam_idx = q.lam_idx;
+  if (ev) LGB_CUDA(cudaEventRecord(ev[0], s));
+  if ((st = launch_stage<BN>(p, q.bf16, m1, s))) return st;
+  if (ev) LGB_CUDA(cudaEventRecord(ev[1], s));
+
+  p.stage = 2;
+  p.kblocks = sh[1].kblocks;
+  p.m_tiles = cdiv(q.M, 2 * BM);
+  p.n_tiles = cdiv(q.N, BN / 2);                        // BN/2 complex columns per tile
+  p.n_last = BN;                                        // E2 blocks are padded to whole tiles
+  p.n_items = (int)sh[1].items;
+  p.epilogue = q.epilogue;
+  p.weights = q.weights;
+  p.unit2 = q.unit2;
+  p.wbuf = q.wbuf;
+  p.ldw = q.ldw;
+  p.out = q.out;
+  p.cscale = q.complex_scale;
+  if (ev) LGB_CUDA(cudaEventRecord(ev[2], s));
+  if ((st = launch_stage<BN>(p, q.bf16, m2, s))) return st;
+  if (ev) LGB_CUDA(cudaEventRecord(ev[3], s));
+  return LGB_OK;
+}
+
+// ------------------------------------------------------------- autotuner ---
+// The tile width is chosen per launch class and cached for the process.  A
+// class is the precision, field m x n, window M x N, epilogue, and the
+// occupancy the problem count gives: the waves of 128-wide tiles of each
+// stage over the resident CTA pairs, capped at 8 (launches of eight or more
+// waves behave alike).
+//
+// The occupancy model below prices both widths.  Where it separates them by
+// TUNE_DECISIVE or more (many waves: the 256-wide tile; a launch far below
+// one wave: the 128-wide one) its choice is final.  In between, measure mode
+// (the default) tunes the class online, on the caller's own launches: the
+// next TUNE_TRIALS launches alternate the two widths, the model's first, each
+// bracketed by CUDA events on its stream; a later launch of the class finds
+// them all finished (cudaEventQuery, no host wait), compares the fastest run
+// of each width, caches the winner and runs with it -- until then it runs the
+// model's width.  No launch is repeated and nothing synchronises.  Both
+// widths' kernels are loaded and configured before a trial is timed, so a
+// first launch's host-side set-up is not charged to its width.  A launch
+// under stream capture uses the cached or the model's width and records
+// nothing.  Model mode takes the model's choice at once; a forced width
+// overrides everything.
+constexpr int TUNE_TRIALS = 4;
+constexpr double TUNE_DECISIVE = 1.4;
+
+struct Trial {
+  int width = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  bool recorded = false;
+};
+struct TuneEntry {
+  int best = 0;              // decided width, 0 while trials run
+  int trials = 0;            // trials handed out (0..TUNE_TRIALS)
+  Trial t[TUNE_TRIALS];
+};
+using TuneKey = std::array<int, 8>;
+struct Tuner {
+  std::mutex mu;
+  std::map<TuneKey, TuneEntry> table;
+  int mode = LGB_TUNE_MEASURE;
+  int forced = 0;
+};
+static Tuner& tuner() {
+  static Tuner* t = new Tuner();     // never destroyed: its events may outlive the CUDA context
+  return *t;
+}
+static thread_local int t_last_tile = 0;
+
+static void drop_trials(TuneEntry& e) {
+  for (Trial& t : e.t) {
+    if (t.e0) cudaEventDestroy(t.e0);
+    if (t.e1) cudaEventDestroy(t.e1);
+    t = Trial();
+  }
+}
+
+static TuneKey tune_key(const SplitMftProblem& q) {
+  const int pairs = std::max(1, sm_count() / 2);
+  StageShape sh[2];
+  stage_shapes(q, 128, sh);
+  auto waves = [&](long long items) { return (int)std::min<long long>(8, (items + pairs - 1) / pairs); };
+  return {q.bf16 ? 1 : 0, q.m, q.n, q.M, q.N, q.epilogue, waves(sh[0].items), waves(sh[1].items)};
+}
+
+// Cost of each width: waves of work items over the resident CTA pairs times
+// K blocks, a 128-wide item costing 0.78 of a 256-wide one (measured on the
+// broadband workload: twice the items took 1.56x the time at full
+// occupancy).  Either width holds one CTA per SM, so the pairs are taken as
+// half the SMs: no occupancy query, which keeps the model usable inside a
+// stream capture.  Returns the cheaper width; *ratio = dearer / cheaper.
+static int model_tile(const SplitMftProblem& q, double* ratio = nullptr) {
+  double cost[2];
+  const int bns[2] = {256, 128};
+  const int pairs = std::max(1, sm_count() / 2);
+  for (int c = 0; c < 2; ++c) {
+    StageShape sh[2];
+    stage_shapes(q, bns[c], sh);
+    cost[c] = 0.0;
+    for (const StageShape& x : sh) cost[c] += (double)((x.items + pairs - 1) / pairs) * x.kblocks;
+    cost[c] *= bns[c] == 256 ? 1.0 : 0.78;
+  }
+  if (ratio) *ratio = std::max(cost[0], cost[1]) / std::max(1e-30, std::min(cost[0], cost[1]));
+  return cost[1] < cost[0] ? 128 : 256;
+}
+
+static int run_tile(const SplitMftProblem& q, int bn, cudaEvent_t* ev, cudaStream_t s) {
+  return bn == 128 ? run_split_mft<128>(q, ev, s) : run_split_mft<256>(q, ev, s);
+}
+
+// Loads and configures both widths' kernels (lazy module load, shared-memory
+// attribute, occupancy) so that no trial is timed across that set-up.
+static void prepare_widths(bool bf16) {
+  if (bf16) { max_pairs<true, 256>(); max_pairs<true, 128>(); }
+  else { max_pairs<false, 256>(); max_pairs<false, 128>(); }
+}
+
+// Width for this launch; ev[0..1] are set when the launch is to be timed
+// (events owned by the tuner's table).
+static int choose_tile(const SplitMftProblem& q, cudaStream_t s, int* bn, cudaEvent_t* ev,
+                       TuneKey* key) {
+  Tuner& T = tuner();
+  ev[0] = ev[1] = nullptr;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  LGB_CUDA(cudaStreamIsCapturing(s, &cap));
+  *key = tune_key(q);
+  double ratio = 1.0;
+  const int model = model_tile(q, &ratio);
+  std::lock_guard<std::mutex> lock(T.mu);
+  if (T.forced) { *bn = T.forced; return LGB_OK; }
+  auto it = T.table.find(*key);
+  if (it != T.table.end() && it->second.best) { *bn = it->second.best; return LGB_OK; }
+  *bn = model;
+  if (cap != cudaStreamCaptureStatusNone) return LGB_OK;
+  if (T.mode == LGB_TUNE_MODEL || ratio >= TUNE_DECISIVE) {
+    T.table[*key].best = model;
+    return LGB_OK;
+  }
+  TuneEntry& e = T.table[*key];
+  if (e.trials < TUNE_TRIALS) {                // hand out the next trial
+    Trial& t = e.t[e.trials];
+    if (cudaEventCreate(&t.e0) != cudaSuccess || cudaEventCreate(&t.e1) != cudaSuccess) {
+      drop_trials(e);
+      e.best = model;                          // cannot time: keep the model's width
+      return LGB_OK;
+    }
+    t.width = (e.trials & 1) == 0 ? model : (model == 256 ? 128 : 256);
+    ++e.trials;
+    *bn = t.width;
+    ev[0] = t.e0;
+    ev[1] = t.e1;
+    return LGB_OK;
+  }
+  float fastest[2] = {1e30f, 1e30f};           // [0]: the model's width, [1]: the other
+  for (int k = 0; k < TUNE_TRIALS; ++k) {
+    const Trial& t = e.t[k];
+    if (!t.recorded) return LGB_OK;            // a trial launch is still being issued
+    const cudaError_t qe = cudaEventQuery(t.e1);
+    if (qe == cudaErrorNotReady) return LGB_OK;
+    float ms = 0.f;
+    if (qe != cudaSuccess || cudaEventElapsedTime(&ms, t.e0, t.e1) != cudaSuccess) {
+      (void)cudaGetLastError();
+      drop_trials(e);
+      e.best = model;
+      return LGB_OK;
+    }
+    float& f = fastest[t.width == model ? 0 : 1];
+    f = std::min(f, ms);
+  }
+  e.best = fastest[1] < fastest[0] ? (model == 256 ? 128 : 256) : model;
+  drop_trials(e);
+  *bn = e.best;
   return LGB_OK;
 }
 
@@ -685,77 +976,92 @@ float split_g_scale(int m) {
 int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
   using namespace tc;
   LGB_REQUIRE(q.kp1 % 32 == 0 && q.kp2 % 32 == 0, LGB_EINVAL, "split mft: K padding");
-  const int Q = q.batch * q.L;
-  const int mrows1 = cdiv(q.M, 64) * 128;      // E1 block rows
-  const int nrows2 = cdiv(q.N, 128) * 256;     // E2 block rows
-  const uint32_t idesc = make_idesc(q.bf16);
-  CUtensorMap a_hi, a_lo, b_hi, b_lo, c0, c1;
-  int st;
-
-  // ---- stage 1: G = E1 . f
-  const int Lm = q.lam_idx ? q.L_bank : q.L;     // DFT-matrix slots held
-  if ((st = make_map(&a_hi, q.e1_hi, q.bf16, 2 * q.kp1, mrows1, Lm, BM))) return st;
-  if ((st = make_map(&a_lo, q.e1_lo, q.bf16, 2 * q.kp1, mrows1, Lm, BM))) return st;
-  if ((st = make_map(&b_hi, q.f_hi, q.bf16, 2 * q.kp1, q.n, Q, BNC))) return st;
-  if ((st = make_map(&b_lo, q.f_lo, q.bf16, 2 * q.kp1, q.n, Q, BNC))) return st;
-  if ((st = make_map_any(&c0, q.g_hi, half_type(q.bf16), 2, 2 * q.kp2, q.M, Q, 32, 32,
-                         CU_TENSOR_MAP_SWIZZLE_64B)))
-    return st;
-  if ((st = make_map_any(&c1, q.g_lo, half_type(q.bf16), 2, 2 * q.kp2, q.M, Q, 32, 32,
-                         CU_TENSOR_MAP_SWIZZLE_64B)))
-    return st;
-  Params p{};
-  p.stage = 1;
-  p.kblocks = 2 * q.kp1 / BK;
-  p.m_tiles = cdiv(cdiv(q.M, 64), 2);          // pairs of 64-row (128 block-row) E1 tiles
-  p.n_tiles = cdiv(q.kp2, BN);
-  p.n_items = Q * p.m_tiles * p.n_tiles;
-  p.L = q.L;
-  p.idesc = idesc;
-  p.M = q.M; p.N = q.N;
-  p.kp_out = q.kp2;
-  p.n_last = q.kp2 - (p.n_tiles - 1) * BN;              // kp2 % 32 == 0, so n_last % 32 == 0
-  p.sG = split_g_scale(q.m);
-  p.g_hi = q.g_hi; p.g_lo = q.g_lo;
-  p.maxabs = q.maxabs;
-  p.err = q.err;
-  p.lam_idx = q.lam_idx;
-  if (q.events) LGB_CUDA(cudaEventRecord(q.events[0], s));
-  st = q.bf16 ? launch_one<true>(p, a_hi, a_lo, b_hi, b_lo, c0, c1, s)
-              : launch_one<false>(p, a_hi, a_lo, b_hi, b_lo, c0, c1, s);
-  if (st) return st;
-  if (q.events) LGB_CUDA(cudaEventRecord(q.events[1], s));
-
-  // ---- stage 2: F = G . E2 (+ epilogue)
-  if ((st = make_map(&a_hi, q.g_hi, q.bf16, 2 * q.kp2, q.M, Q, BM))) return st;
-  if ((st = make_map(&a_lo, q.g_lo, q.bf16, 2 * q.kp2, q.M, Q, BM))) return st;
-  if ((st = make_map(&b_hi, q.e2_hi, q.bf16, 2 * q.kp2, nrows2, Lm, BNC))) return st;
-  if ((st = make_map(&b_lo, q.e2_lo, q.bf16, 2 * q.kp2, nrows2, Lm, BNC))) return st;
-  if (q.epilogue == 0) {
-    LGB_REQUIRE(q.ldw % 4 == 0, LGB_EINVAL, "split mft: intensity window pitch must be a multiple of 4");
-    if ((st = make_map_any(&c0, q.wbuf, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, q.ldw, q.M, q.batch, 32, 32,
-                           CU_TENSOR_MAP_SWIZZLE_128B)))
-      return st;
+  int bn = q.tile;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  TuneKey key{};
+  if (bn != 0) {                               // a forced width overrides the caller's too
+    Tuner& T = tuner();
+    std::lock_guard<std::mutex> lock(T.mu);
+    if (T.forced) bn = T.forced;
+  } else {
+    const int st = choose_tile(q, s, &bn, ev, &key);
+    if (st) return st;
   }
-  p.stage = 2;
-  p.kblocks = 2 * q.kp2 / BK;
-  p.m_tiles = cdiv(q.M, 2 * BM);
-  p.n_tiles = cdiv(q.N, 128);
-  p.n_last = BN;                                        // E2 blocks are padded to whole tiles
-  p.n_items = Q * p.m_tiles * p.n_tiles;
-  p.epilogue = q.epilogue;
-  p.weights = q.weights;
-  p.unit2 = q.unit2;
-  p.wbuf = q.wbuf;
-  p.ldw = q.ldw;
-  p.out = q.out;
-  p.cscale = q.complex_scale;
-  if (q.events) LGB_CUDA(cudaEventRecord(q.events[2], s));
-  st = q.bf16 ? launch_one<true>(p, a_hi, a_lo, b_hi, b_lo, c0, c1, s)
-              : launch_one<false>(p, a_hi, a_lo, b_hi, b_lo, c0, c1, s);
+  LGB_REQUIRE(bn == 256 || bn == 128, LGB_EINVAL, "split mft: tile width must be 256 or 128");
+  t_last_tile = bn;
+  // a timed trial brackets the launch with the entry's events (a concurrent
+  // lgb_tuner_clear may have destroyed them: the launch then runs untimed)
+  if (ev[0]) prepare_widths(q.bf16);
+  bool timed = ev[0] && cudaEventRecord(ev[0], s) == cudaSuccess;
+  if (ev[0] && !timed) (void)cudaGetLastError();   // not the launch's error: clear it
+  const int st = run_tile(q, bn, q.events, s);
   if (st) return st;
-  if (q.events) LGB_CUDA(cudaEventRecord(q.events[3], s));
+  if (timed && cudaEventRecord(ev[1], s) != cudaSuccess) {
+    (void)cudaGetLastError();
+    timed = false;
+  }
+  if (timed) {
+    Tuner& T = tuner();
+    std::lock_guard<std::mutex> lock(T.mu);
+    auto it = T.table.find(key);
+    if (it != T.table.end())
+      for (Trial& t : it->second.t)
+        if (t.e1 == ev[1]) t.recorded = true;
+  }
   return LGB_OK;
 }
 
 }  // namespace lgb
+
+// ------------------------------------------------------------- tuner ABI ---
+using namespace lgb;
+
+extern "C" int lgb_tuner_set_mode(int mode) {
+  LGB_REQUIRE(mode == LGB_TUNE_MODEL || mode == LGB_TUNE_MEASURE, LGB_EINVAL,
+              "tuner_set_mode: mode must be LGB_TUNE_MODEL or LGB_TUNE_MEASURE");
+  tc::Tuner& T = tc::tuner();
+  std::lock_guard<std::mutex> lock(T.mu);
+  T.mode = mode;
+  return LGB_OK;
+}
+
+extern "C" int lgb_tuner_force_tile(int tile) {
+  LGB_REQUIRE(tile == 0 || tile == 128 || tile == 256, LGB_EINVAL,
+              "tuner_force_tile: tile must be 0 (tuned), 128 or 256");
+  tc::Tuner& T = tc::tuner();
+  std::lock_guard<std::mutex> lock(T.mu);
+  T.forced = tile;
+  return LGB_OK;
+}
+
+extern "C" void lgb_tuner_clear(void) {
+  tc::Tuner& T = tc::tuner();
+  std::lock_guard<std::mutex> lock(T.mu);
+  for (auto& kv : T.table) tc::drop_trials(kv.second);
+  T.table.clear();
+}
+
+extern "C" int lgb_tuner_entries(void) {
+  tc::Tuner& T = tc::tuner();
+  std::lock_guard<std::mutex> lock(T.mu);
+  int n = 0;
+  for (const auto& kv : T.table) n += kv.second.best != 0;
+  return n;
+}
+
+extern "C" int lgb_tuner_lookup(int m, int n, int M, int N, int count, int precision, int epilogue) {
+  if (m <= 0 || n <= 0 || M <= 0 || N <= 0 || count <= 0) return 0;
+  SplitMftProblem q{};
+  q.bf16 = precision == LGB_SPLIT_BF16;
+  q.m = m; q.n = n; q.M = M; q.N = N;
+  q.kp1 = round_up(m, 32); q.kp2 = round_up(n, 32);
+  q.L = count; q.batch = 1;
+  q.epilogue = epilogue;
+  const tc::TuneKey key = tc::tune_key(q);
+  tc::Tuner& T = tc::tuner();
+  std::lock_guard<std::mutex> lock(T.mu);
+  const auto it = T.table.find(key);
+  return it == T.table.end() ? 0 : it->second.best;
+}
+
+extern "C" int lgb_tuner_last_tile(void) { return tc::t_last_tile; }

@@ -270,6 +270,7 @@ struct lgb_psf_plan_s {
   // split
   uint16_t *e1h = nullptr, *e1l = nullptr, *e2h = nullptr, *e2l = nullptr;
   SplitOperands ops;               // plan-owned operands (batch > 0)
+  int tile = 0;                    // tensor-core pair-tile width: 0 = the autotuner's, 128, 256
   // optional per-kernel timing: event pairs recorded around each launch
   bool profile = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -464,6 +465,7 @@ static int psf_execute_n(lgb_psf_plan P, int B, const int* lam_idx, int n_sel, c
     p.wbuf = ops.wbuf;
     p.ldw = ops.ldw;
     p.err = errp;
+    p.tile = P->tile;
     LGB_CUDA(cudaMemsetAsync(ops.wbuf, 0, sizeof(float) * (size_t)B * d.M * ops.ldw, s));
     cudaEvent_t mev[4];
     if (P->profile) {
@@ -550,6 +552,14 @@ extern "C" int lgb_psf_execute_subset(lgb_psf_plan P, int count, const int* lam_
                                       double* out, int accumulate, lgb_stream stream) {
   LGB_REQUIRE(lam_idx, LGB_EINVAL, "psf_execute_subset: null wavelength index");
   return psf_execute_n(P, count, lam_idx, n_sel, amp, opd, weights, out, accumulate, stream);
+}
+
+extern "C" int lgb_psf_plan_set_tile(lgb_psf_plan P, int tile) {
+  LGB_REQUIRE(P, LGB_EINVAL, "psf_plan_set_tile: null plan");
+  LGB_REQUIRE(tile == 0 || tile == 128 || tile == 256, LGB_EINVAL,
+              "psf_plan_set_tile: tile must be 0 (tuned), 128 or 256");
+  P->tile = tile;
+  return LGB_OK;
 }
 
 extern "C" int lgb_psf_plan_profile(lgb_psf_plan P, int enable) {

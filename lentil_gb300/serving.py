@@ -17,8 +17,13 @@ weights, optics) are queued by any thread and scheduled by one GPU thread:
   so requests that arrive while others run are admitted as streams free up,
   and launches (of the same plan or of different plans) overlap on the
   device;
+- a launch issued while others are in flight shares the GPU, so it runs the
+  tensor-core tile with the best throughput per SM (256 columns); a launch
+  issued onto an idle GPU takes the autotuner's width for its launch class
+  (``lentil_gb300.tuner``), which may be the narrower tile when it alone
+  cannot occupy every CTA pair;
 - a small launch shape seen twice keeps its buffers and is captured into a
-  CUDA graph that later launches replay;
+  CUDA graph (one per tile width) that later launches replay;
 - completion is detected with CUDA events; latency is submit -> result.
 """
 import collections
@@ -101,7 +106,7 @@ class _Buffers:
         self.hW = torch.empty(n * n_sel, dtype=torch.float64, pin_memory=True)
         self.hlam = torch.empty(n_sel, dtype=torch.int32, pin_memory=True)
         self.hout = torch.empty((n,) + slot.geo.shape_out, dtype=torch.float64, pin_memory=True)
-        self.graph = None
+        self.graphs = {}              # tile width -> captured launch
         self.busy = False
 
     @property
@@ -141,23 +146,26 @@ class _Slot:
             return b, True
         return b, False
 
-    def run(self, b, stream, reuse):
-        """Launch buffers ``b`` (host inputs already staged) on ``stream``."""
+    def run(self, b, stream, reuse, tile):
+        """Launch buffers ``b`` (host inputs already staged) on ``stream``
+        with pair-tile width ``tile`` (0: the autotuner's)."""
         n, n_sel = b.n, b.n_sel
+        self.plan.set_tile(tile)
         with torch.cuda.stream(stream):
             b.A.copy_(b.hA, non_blocking=True)
             b.O.copy_(b.hO, non_blocking=True)
             b.Wt.copy_(b.hW, non_blocking=True)
             if self.grid:
                 b.lam.copy_(b.hlam, non_blocking=True)
-            if reuse and b.graph is None:
+            g = b.graphs.get(tile)
+            if reuse and g is None:
                 b.launch(self)                       # warm-up outside capture
                 g = torch.cuda.CUDAGraph()
                 with torch.cuda.graph(g, stream=stream):
                     b.launch(self)
-                b.graph = g
-            if b.graph is not None:
-                b.graph.replay()
+                b.graphs[tile] = g
+            if g is not None:
+                g.replay()
             else:
                 b.launch(self)
             b.hout.copy_(b.out, non_blocking=True)
@@ -171,6 +179,8 @@ class PSFServer:
 
     ``grid``: the spectral grid (metres) whose wavelengths share resident DFT
     matrices; default 128 points over 400-1000 nm."""
+
+    SHARED_TILE = 256     # tile width of launches issued while others are in flight
 
     def __init__(self, hbm_budget=None, streams=4, max_batch=4, precision='split',
                  use_graphs=True, grid=None, device=None):
@@ -379,11 +389,13 @@ class PSFServer:
             si = self._free_streams.pop(0)
             b.busy = True
             slot.inflight += 1
-            ev = slot.run(b, self._streams[si], reuse)
+            tile = self.SHARED_TILE if self._inflight else 0
+            ev = slot.run(b, self._streams[si], reuse, tile)
             self._inflight.append((ev, slot, b, batch, si))
             self.stats['launches'] += 1
             self.stats['batched'] += len(batch)
-            if b.graph is not None:
+            self.stats['tuned_tile_launches' if tile == 0 else 'shared_gpu_launches'] += 1
+            if tile in b.graphs:
                 self.stats['graph_launches'] += 1
             progressed = True
         return progressed

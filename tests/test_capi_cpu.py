@@ -82,5 +82,17 @@ def test_pixel_workspace_covers_off_grid_buffers(lib, n, os_):
     assert lib.lgb_pixelate_size(0, 2) == -1 and lib.lgb_pixelate_size(10, 0) == -1
 
 
+def test_tuner_controls_without_a_gpu(lib):
+    # mode / forced width / cache controls touch no device
+    assert lib.lgb_tuner_set_mode(0) == _lib.OK and lib.lgb_tuner_set_mode(1) == _lib.OK
+    assert lib.lgb_tuner_set_mode(7) == _lib.EINVAL
+    assert lib.lgb_tuner_force_tile(128) == _lib.OK and lib.lgb_tuner_force_tile(0) == _lib.OK
+    assert lib.lgb_tuner_force_tile(96) == _lib.EINVAL
+    lib.lgb_tuner_clear()
+    assert lib.lgb_tuner_entries() == 0
+    assert lib.lgb_tuner_lookup(64, 64, 64, 64, 1, _lib.SPLIT_BF16, 0) == 0
+    assert lib.lgb_tuner_last_tile() == 0
+
+
 def test_build_is_up_to_date():
     assert _build.up_to_date()

@@ -45,6 +45,10 @@ def test_results_same_alone_and_in_mix(cuda_device):
     assert stats['completed'] == len(reqs)
     assert stats['batched'] == len(reqs)
     assert stats['launches'] < len(reqs)          # same-plan requests were batched
+    # every launch either had the GPU to itself (autotuned tile width) or
+    # shared it with launches in flight (the 256-wide throughput tile)
+    assert stats['tuned_tile_launches'] + stats['shared_gpu_launches'] == stats['launches']
+    assert stats['tuned_tile_launches'] >= 1      # the first launch found the GPU idle
     for r, img in zip(reqs, results):
         ref = _alone(r)
         assert img.shape == ref.shape
