@@ -566,11 +566,23 @@ def run_phase_retrieval(args):
                   for x in t]
     c = torch.zeros(len(sigma), dtype=torch.float64, device='cuda', requires_grad=True)
 
-    def step():
+    def eager():
         c.grad = None
         pr.loss(c).backward()
 
+    def step():                                     # loss + gradient replayed from CUDA graphs
+        c.grad = None
+        pr.graphed_loss(c).backward()
+
+    e_mean, e_p50, e_p99 = _timed(eager, args.steps, args.warmup)
     mean, p50, p99 = _timed(step, args.steps, args.warmup)
+    c.grad = None
+    pr.graphed_loss(c).backward()
+    g_graph = c.grad.clone()
+    c.grad = None
+    pr.loss(c).backward()
+    grad_rel = float((g_graph - c.grad).abs().max() / c.grad.abs().max())
+    pr.check()
     m, n = g.slc[2], g.slc[3]
     M, N = g.shape
     flops = 3 * 8.0 * (M * m * n + M * n * N) * 3      # forward + recompute + adjoint, 3 images
@@ -580,7 +592,11 @@ def run_phase_retrieval(args):
             'higher_is_better': True, 'dtype': args.precision, 'data': 'synthetic (seeded)',
             'config': {'workload': '512^2 circular pupil, Noll 2-37 + 18-segment PTT, 3 diversity '
                                    'images at -1/0/+1 wave defocus, 633 nm, 256^2 detector x2',
-                       'parameters': int(len(sigma)), 'mft_tile': tuner_summary(args)},
+                       'parameters': int(len(sigma)), 'mft_tile': tuner_summary(args),
+                       'path': 'PhaseRetrieval.graphed_loss (forward and backward CUDA graphs)'},
+            'eager': {'value': 1e3 / e_mean, 'p50_ms': e_p50, 'p99_ms': e_p99,
+                      'path': 'PhaseRetrieval.loss (eager autograd)'},
+            'graph_vs_eager_grad_rel_diff': grad_rel,
             'mft_tflops_algorithmic': flops / (mean / 1e3) / 1e12}
     print(json.dumps(line), flush=True)
 

@@ -84,6 +84,39 @@ int lgb_dft2_batch(const lgb_c128* f, int count, int m, int n, lgb_c128* F, int 
                    double offset_r, double offset_c, int unitary, int precision,
                    void* workspace, size_t workspace_bytes, lgb_stream stream);
 
+/* dft2 plans (an extension; lentil rebuilds its DFT matrices on every
+ * call): one geometry (m, n, M, N, alpha, shift, offset, unitary,
+ * precision) with its DFT matrices built at creation and kept on the
+ * device (lgb_dft2_plan_bytes).  lgb_dft2_plan_execute transforms `count`
+ * fields f[count][m][n] -> F[count][M][N] with no matrix build, no host
+ * copy and no host wait; its workspace holds
+ * lgb_dft2_plan_workspace_size(plan, count) bytes (256-byte aligned) and
+ * one plan may run on several streams at once.  Status of the split path:
+ * each execute copies the plan's sticky device flag to pinned host memory
+ * behind an event, and the next execute returns LGB_ETIMEOUT if that copy
+ * has landed and shows an expired wait (nothing is copied or queried under
+ * stream capture); lgb_dft2_plan_status waits and reports at once.
+ * Creation issues no host wait.  lgb_dft2_plan_create allocates the plan's
+ * device memory (lgb_dft2_plan_destroy then waits for the device before
+ * freeing it); lgb_dft2_plan_create_in builds it in caller-owned device
+ * memory of lgb_dft2_plan_size bytes (256-byte aligned), which destroy does
+ * not touch: the caller keeps it alive until the plan's executes are done. */
+typedef struct lgb_dft2_plan_s* lgb_dft2_plan;
+size_t lgb_dft2_plan_size(int m, int n, int M, int N, int precision);
+int lgb_dft2_plan_create(int m, int n, int M, int N, double alpha_r, double alpha_c,
+                         double shift_r, double shift_c, double offset_r, double offset_c,
+                         int unitary, int precision, lgb_stream stream, lgb_dft2_plan* plan);
+int lgb_dft2_plan_create_in(int m, int n, int M, int N, double alpha_r, double alpha_c,
+                            double shift_r, double shift_c, double offset_r, double offset_c,
+                            int unitary, int precision, void* memory, size_t memory_bytes,
+                            lgb_stream stream, lgb_dft2_plan* plan);
+size_t lgb_dft2_plan_bytes(lgb_dft2_plan plan);
+size_t lgb_dft2_plan_workspace_size(lgb_dft2_plan plan, int count);
+int lgb_dft2_plan_execute(lgb_dft2_plan plan, const lgb_c128* f, int count, lgb_c128* F,
+                          void* workspace, size_t workspace_bytes, lgb_stream stream);
+int lgb_dft2_plan_status(lgb_dft2_plan plan, lgb_stream stream);
+int lgb_dft2_plan_destroy(lgb_dft2_plan plan);
+
 /* ------------------------------------------------------------------------
  * Allocation-free complex128 dft2 (no counterpart in lentil: an addition of
  * this library for callers that may not allocate device memory at call time,

@@ -61,6 +61,19 @@ SIGNATURES = {
     'lgb_pixel': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t, c_void_p]),
     'lgb_pixelate_size': (c_int, [c_int, c_int]),
     'lgb_psf_plan_set_tile': (c_int, [c_void_p, c_int]),
+    'lgb_dft2_plan_create': (c_int, [c_int, c_int, c_int, c_int, c_double, c_double, c_double,
+                                     c_double, c_double, c_double, c_int, c_int, c_void_p,
+                                     ctypes.POINTER(c_void_p)]),
+    'lgb_dft2_plan_size': (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
+    'lgb_dft2_plan_create_in': (c_int, [c_int, c_int, c_int, c_int, c_double, c_double, c_double,
+                                        c_double, c_double, c_double, c_int, c_int, c_void_p,
+                                        c_size_t, c_void_p, ctypes.POINTER(c_void_p)]),
+    'lgb_dft2_plan_bytes': (c_size_t, [c_void_p]),
+    'lgb_dft2_plan_workspace_size': (c_size_t, [c_void_p, c_int]),
+    'lgb_dft2_plan_execute': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_size_t,
+                                      c_void_p]),
+    'lgb_dft2_plan_status': (c_int, [c_void_p, c_void_p]),
+    'lgb_dft2_plan_destroy': (c_int, [c_void_p]),
     'lgb_tuner_set_mode': (c_int, [c_int]),
     'lgb_tuner_force_tile': (c_int, [c_int]),
     'lgb_tuner_clear': (None, []),

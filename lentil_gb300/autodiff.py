@@ -108,7 +108,16 @@ def mft_intensity(opd, amp, g):
 class PhaseRetrieval:
     """Focus-diverse phase-retrieval loss sum_k sum (PSF_k - target_k)^2 over
     OPD = basis . coeffs (+ an optional free-form map), with the diversity
-    OPD maps added per image."""
+    OPD maps added per image.
+
+    ``loss`` runs eagerly.  ``graphed_loss`` is the same function of the
+    coefficients captured once as two CUDA graphs (forward, backward) with
+    ``torch.cuda.make_graphed_callables`` and replayed on later calls: the
+    transforms run from cached, pinned dft2 plans and every launch goes to
+    the current stream, so a replay issues no host work per kernel.  The
+    diversity maps, targets and basis are read where they lie when the graphs
+    are captured (assign new targets in place).  ``check()`` raises a
+    device-side failure of the transforms."""
 
     def __init__(self, amp, basis, diversity, targets, g):
         dev = dv.device()
@@ -118,6 +127,8 @@ class PhaseRetrieval:
         self.targets = [dv.to_device(t, torch.float64) for t in targets]
         self.g = g
         self.device = dev
+        self._graphed = None
+        self._pins = None
 
     def opd(self, coeffs, free=None):
         o = torch.einsum('k,khw->hw', coeffs, self.basis)
@@ -127,3 +138,31 @@ class PhaseRetrieval:
         o = self.opd(coeffs, free)
         stack = o.unsqueeze(0) + torch.stack(self.diversity)   # all images in one batched MFT
         return ((mft_intensity(stack, self.amp, self.g) - torch.stack(self.targets)) ** 2).sum()
+
+    def graphed_loss(self, coeffs):
+        """``loss(coeffs)`` replayed from CUDA graphs (captured on first use)."""
+        if self._graphed is None:
+            div = torch.stack(self.diversity)
+            tgt = torch.stack(self.targets)
+
+            def fn(c):
+                o = torch.einsum('k,khw->hw', c, self.basis)
+                return ((mft_intensity(o.unsqueeze(0) + div, self.amp, self.g) - tgt) ** 2).sum()
+
+            sample = coeffs.detach().clone().requires_grad_(True)
+            with fourier.pinned_plans() as pins:
+                self._graphed = torch.cuda.make_graphed_callables(fn, (sample,))
+            self._pins = pins
+            self._static = (div, tgt)
+        return self._graphed(coeffs)
+
+    def release_graphs(self):
+        """Drop the captured graphs and unpin their dft2 plans."""
+        self._graphed = None
+        if self._pins is not None:
+            self._pins.release()
+            self._pins = None
+
+    def check(self):
+        """Wait for the device and raise a failure of a split-precision transform."""
+        fourier.plan_status()

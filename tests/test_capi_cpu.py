@@ -94,5 +94,18 @@ def test_tuner_controls_without_a_gpu(lib):
     assert lib.lgb_tuner_last_tile() == 0
 
 
+def test_dft2_plan_argument_errors_without_a_gpu(lib):
+    # invalid geometries are rejected before any device call
+    h = ctypes.c_void_p()
+    assert lib.lgb_dft2_plan_create(0, 4, 4, 4, .1, .1, 0, 0, 0, 0, 1, 0, None,
+                                    ctypes.byref(h)) == _lib.EINVAL
+    assert lib.lgb_dft2_plan_create(4, 4, 4, 4, .1, .1, 0, 0, 0, 0, 1, 9, None,
+                                    ctypes.byref(h)) == _lib.EINVAL
+    assert not h.value
+    assert lib.lgb_dft2_plan_bytes(None) == 0 and lib.lgb_dft2_plan_workspace_size(None, 1) == 0
+    assert lib.lgb_dft2_plan_destroy(None) == _lib.OK
+    assert lib.lgb_dft2_plan_execute(None, None, 1, None, None, 0, None) == _lib.EINVAL
+
+
 def test_build_is_up_to_date():
     assert _build.up_to_date()

@@ -142,3 +142,53 @@ def test_stacked_images_match_single_images(cuda_device, precision):
     assert abs(L.item() - total) <= tol * abs(total)
     gs = np.stack(grads)
     assert np.max(np.abs(o.grad.cpu().numpy() - gs)) <= tol * np.max(np.abs(gs))
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split-bf16'])
+def test_graphed_loss_matches_eager(cuda_device, precision):
+    # the loss and coefficient gradient replayed from CUDA graphs equal the
+    # eager evaluation, across several replays with different coefficients;
+    # the captured transforms' plans stay cached until the graphs are released
+    npix = 64
+    amp = lo.normalize_power(lg.circle((npix, npix), npix * 0.45))
+    basis = np.asarray([lg.zernike(amp > 0, j) for j in range(2, 16)])
+    g = autodiff.geometry(amp, 633e-9, 1.0 / npix, 10.0, 5e-6 * 4, shape=24, oversample=2,
+                          precision=precision)
+    z4 = lg.zernike(amp > 0, 4)
+    div = [k * 633e-9 / (z4.max() - z4.min()) * z4 for k in (-1, 0, 1)]
+    rng = np.random.default_rng(8)
+    tg = [rng.uniform(0, 1e-3, g.shape) for _ in range(3)]
+    pr = autodiff.PhaseRetrieval(amp, basis, div, tg, g)
+    lg.fourier.clear_plan_cache()
+    c = torch.zeros(len(basis), dtype=torch.float64, device='cuda', requires_grad=True)
+    for trial in range(3):
+        with torch.no_grad():
+            c.copy_(torch.as_tensor(rng.normal(0, 20e-9, len(basis)), device='cuda'))
+        c.grad = None
+        Lg = pr.graphed_loss(c)
+        Lg.backward()
+        gg = c.grad.clone()
+        c.grad = None
+        Le = pr.loss(c)
+        Le.backward()
+        assert abs(Lg.item() - Le.item()) <= 1e-12 * abs(Le.item()), trial
+        assert torch.allclose(gg, c.grad, rtol=1e-10, atol=1e-12 * gg.abs().max().item()), trial
+    n_pinned = lg.fourier.plan_cache_info()[0]
+    assert n_pinned >= 2                        # forward and adjoint geometries
+    old = lg.fourier.PLAN_CACHE_ENTRIES
+    try:
+        lg.fourier.PLAN_CACHE_ENTRIES = 1       # pinned plans are not evicted
+        f = rng.standard_normal((20, 20)) + 0j
+        for _ in range(2):
+            lg.fourier.dft2(f, 0.05, precision=precision)
+        assert lg.fourier.plan_cache_info()[0] == n_pinned + 1
+        c.grad = None
+        pr.graphed_loss(c).backward()           # replays on the pinned plans
+        g2 = c.grad.clone()
+        c.grad = None
+        pr.loss(c).backward()
+        assert torch.allclose(g2, c.grad, rtol=1e-10, atol=1e-12 * g2.abs().max().item())
+    finally:
+        lg.fourier.PLAN_CACHE_ENTRIES = old
+    pr.check()
+    pr.release_graphs()

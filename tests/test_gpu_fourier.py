@@ -152,3 +152,64 @@ def test_dft2_batch_matches_single_and_oracle(cuda_device, precision):
     assert isinstance(T, torch.Tensor) and T.is_cuda
     with pytest.raises(ValueError):
         lg.fourier.dft2_batch(f[0], alpha, precision=precision, **kw)
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split-bf16'])
+def test_plan_cache_reuses_and_evicts(cuda_device, precision):
+    # a geometry's first transform runs without a plan, its second creates
+    # one (DFT matrices resident), later ones reuse it; LRU eviction beyond
+    # the entry bound; every path gives the same transform
+    fourier = lg.fourier
+    fourier.clear_plan_cache()
+    rng = np.random.default_rng(9)
+    f = rng.standard_normal((40, 36)) + 1j * rng.standard_normal((40, 36))
+    kw = dict(shape=(48, 30), shift=(0.5, -1), offset=(1, 2), precision=precision)
+    tol = FP64_TOL if precision == 'fp64' else SPLIT_TOL[precision]
+    same = (lambda x, y: np.array_equal(x, y)) if precision == 'fp64' else \
+        (lambda x, y: lo.peak_normalised_error(x, y) < 1e-12)   # tile widths may differ
+    a = fourier.dft2(f, 0.02, **kw)
+    assert fourier.plan_cache_info()[0] == 0
+    b = fourier.dft2(f, 0.02, **kw)
+    assert fourier.plan_cache_info()[0] == 1 and same(a, b)
+    c = fourier.dft2(f, 0.02, **kw)
+    assert fourier.plan_cache_info()[0] == 1 and same(b, c)
+    ref = lo.dft2(f, 0.02, **{k: v for k, v in kw.items() if k != 'precision'})
+    assert lo.peak_normalised_error(c, ref) < tol
+    old = fourier.PLAN_CACHE_ENTRIES
+    try:
+        fourier.PLAN_CACHE_ENTRIES = 2
+        for alpha in (0.021, 0.021, 0.022, 0.022):   # two more plans: the 0.02 one goes
+            fourier.dft2(f, alpha, **kw)
+        assert fourier.plan_cache_info()[0] == 2
+        for _ in range(2):
+            assert same(fourier.dft2(f, 0.02, **kw), a)
+        assert fourier.plan_cache_info()[0] == 2
+    finally:
+        fourier.PLAN_CACHE_ENTRIES = old
+    fourier.plan_status()
+    fourier.clear_plan_cache()
+    assert fourier.plan_cache_info() == (0, 0)
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split-fp16'])
+def test_cached_plan_replays_under_graph_capture(cuda_device, precision):
+    # a cached geometry transforms with no allocation-free-path restrictions
+    # but no host copy either, so it can be captured into a CUDA graph
+    fourier = lg.fourier
+    rng = np.random.default_rng(10)
+    f = torch.as_tensor(rng.standard_normal((2, 64, 50)) + 1j * rng.standard_normal((2, 64, 50)),
+                        device='cuda')
+    kw = dict(shape=(40, 44), shift=(0.25, 0.5), precision=precision)
+    ref = fourier.dft2_batch(f, (0.015, 0.018), **kw)       # first use: no plan yet
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        fourier.dft2_batch(f, (0.015, 0.018), **kw)         # second use: creates the plan
+        with torch.cuda.graph(g, stream=s):
+            out = fourier.dft2_batch(f, (0.015, 0.018), **kw)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)
+    fourier.plan_status()
