@@ -21,8 +21,17 @@ def is_tensor(x):
     return isinstance(x, torch.Tensor)
 
 
+PINNED_COPY_LIMIT = 64 << 20     # host arrays up to this size are staged through pinned memory
+
+
 def to_device(x, dtype):
-    """numpy / scalar / tensor -> contiguous CUDA tensor of ``dtype`` (one copy at most)."""
+    """numpy / scalar / tensor -> contiguous CUDA tensor of ``dtype`` (one copy at most).
+
+    Host data never makes the host wait for the GPU: a single value becomes a
+    device fill (no copy), an array up to ``PINNED_COPY_LIMIT`` is copied into
+    a pinned block of torch's caching host allocator (read before this call
+    returns, so the caller may reuse its array) and sent with an asynchronous
+    copy on the current stream."""
     dev = device()
     if is_tensor(x):
         t = x.to(device=dev, dtype=dtype)
@@ -32,9 +41,15 @@ def to_device(x, dtype):
             a = a.astype(np.complex128, copy=False)
         elif dtype == torch.float64:
             a = a.astype(np.float64, copy=False)
+        if a.size == 1 and a.dtype.kind in 'fc':
+            return torch.full(a.shape, a.item(), dtype=dtype, device=dev)
         # np.ascontiguousarray would turn a 0-d array into shape (1,)
         a = a if a.flags.c_contiguous else a.copy(order='C')
-        t = torch.from_numpy(a).to(device=dev, dtype=dtype)
+        h = torch.from_numpy(a)
+        if 0 < a.nbytes <= PINNED_COPY_LIMIT and h.dtype == dtype:
+            t = h.pin_memory().to(device=dev, non_blocking=True)
+        else:
+            t = h.to(device=dev, dtype=dtype)
     return t.contiguous()
 
 

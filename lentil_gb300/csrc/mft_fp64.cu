@@ -2,6 +2,9 @@
 // (lentil/fourier.py:95-101), as two tiled complex GEMMs on the FP64 pipe.
 // This is the parity form (<= 1e-12 peak-normalised against numpy) and the
 // baseline the split tensor-core form is measured against.
+#include <algorithm>
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -9,34 +12,39 @@ namespace lgb {
 
 constexpr int ZBM = 64, ZBN = 64, ZBK = 16;
 
+// blockIdx.z = b * splits + split: problem b, K range [split * kchunk,
+// (split + 1) * kchunk); with splits > 1 each split writes its own partial
+// product (C offset by split * sP) for zgemm_reduce_kernel to sum in order.
 __global__ void __launch_bounds__(256) zgemm_kernel(int M, int N, int K,
                                                     const double2* __restrict__ A, int lda, long long sA,
                                                     const double2* __restrict__ B, int ldb, long long sB,
                                                     double2* __restrict__ C, int ldc, long long sC,
-                                                    double alpha) {
+                                                    double alpha, int splits, int kchunk, long long sP) {
   __shared__ double2 As[ZBK][ZBM];
   __shared__ double2 Bs[ZBK][ZBN];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4, tid = threadIdx.x;
   const int m0 = blockIdx.y * ZBM, n0 = blockIdx.x * ZBN;
-  A += (size_t)blockIdx.z * sA;
-  B += (size_t)blockIdx.z * sB;
-  C += (size_t)blockIdx.z * sC;
+  const int b = blockIdx.z / splits, split = blockIdx.z - b * splits;
+  A += (size_t)b * sA;
+  B += (size_t)b * sB;
+  C += (size_t)b * sC + (size_t)split * sP;
+  const int kbeg = split * kchunk, kend = min(K, kbeg + kchunk);
   double cr[4][4], ci[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) cr[i][j] = ci[i][j] = 0.0;
 
-  for (int k0 = 0; k0 < K; k0 += ZBK) {
+  for (int k0 = kbeg; k0 < kend; k0 += ZBK) {
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int e = tid + 256 * t;
       const int ar = e >> 4, ak = e & 15;          // A tile: 64 rows x 16 k
       const int gr = m0 + ar, gk = k0 + ak;
-      As[ak][ar] = (gr < M && gk < K) ? A[(size_t)gr * lda + gk] : make_double2(0.0, 0.0);
+      As[ak][ar] = (gr < M && gk < kend) ? A[(size_t)gr * lda + gk] : make_double2(0.0, 0.0);
       const int bk = e >> 6, bc = e & 63;          // B tile: 16 k x 64 cols
       const int hk = k0 + bk, gc = n0 + bc;
-      Bs[bk][bc] = (hk < K && gc < N) ? B[(size_t)hk * ldb + gc] : make_double2(0.0, 0.0);
+      Bs[bk][bc] = (hk < kend && gc < N) ? B[(size_t)hk * ldb + gc] : make_double2(0.0, 0.0);
     }
     __syncthreads();
 #pragma unroll 4
@@ -70,14 +78,83 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int M, int N, int K,
   }
 }
 
+// C[b] = alpha * sum_s P[s][b] in split order (deterministic), P[s][b] M x N dense
+__global__ void zgemm_reduce_kernel(const double2* __restrict__ P, int splits, long long sP,
+                                    int M, int N, double2* __restrict__ C, int ldc, long long sC,
+                                    double alpha) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y, b = blockIdx.z;
+  if (c >= N) return;
+  const double2* p = P + (size_t)b * M * N + (size_t)r * N + c;
+  double re = 0.0, im = 0.0;
+  for (int k = 0; k < splits; ++k) {
+    const double2 v = p[(size_t)k * sP];
+    re += v.x;
+    im += v.y;
+  }
+  C[(size_t)b * sC + (size_t)r * ldc + c] = make_double2(alpha * re, alpha * im);
+}
+
+// The partials come from the device's default stream-ordered pool; by
+// default the pool hands freed memory back at every synchronisation, so the
+// next launch would map it again.  This process keeps up to 256 MiB cached
+// (a property of the process's pool, gone when the process ends).
+static void keep_pool_memory() {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { (void)cudaGetLastError(); return; }
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t keep = (uint64_t)256 << 20;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  (void)cudaGetLastError();
+  done[dev] = true;
+}
+
+// A launch of fewer tiles than SMs would leave the FP64 pipes of most SMs
+// idle (a 256 x 256 output is 16 tiles; each SM retires about two FP64 FMAs
+// a clock), so such a launch splits K over up to 16 CTAs per tile, each
+// writing a partial product to stream-ordered scratch, and a second kernel
+// sums the partials in split order.
 int launch_zgemm(int M, int N, int K, const double2* A, int lda, long long sA, const double2* B,
                  int ldb, long long sB, double2* C, int ldc, long long sC, int batch, double alpha,
                  cudaStream_t s) {
   if (M <= 0 || N <= 0 || batch <= 0) return LGB_OK;
   LGB_REQUIRE(batch <= 65535, LGB_EINVAL, "zgemm: batch too large");
-  dim3 grid(cdiv(N, ZBN), cdiv(M, ZBM), batch);
-  zgemm_kernel<<<grid, 256, 0, s>>>(M, N, K, A, lda, sA, B, ldb, sB, C, ldc, sC, alpha);
-  LGB_CUDA(cudaGetLastError());
+  const long long tiles = (long long)cdiv(N, ZBN) * cdiv(M, ZBM) * batch;
+  const int sms = sm_count();
+  int splits = 1;
+  if (tiles < sms && K > 2 * ZBK)
+    splits = (int)std::min<long long>({(2LL * sms + tiles - 1) / tiles, (long long)cdiv(K, 2 * ZBK), 16LL,
+                                       65535LL / batch});
+  const long long sP = (long long)batch * M * N;          // one split's partials
+  if (splits > 1 && (size_t)splits * sP * sizeof(double2) > ((size_t)256 << 20)) splits = 1;
+  if (splits <= 1) {
+    dim3 grid(cdiv(N, ZBN), cdiv(M, ZBM), batch);
+    zgemm_kernel<<<grid, 256, 0, s>>>(M, N, K, A, lda, sA, B, ldb, sB, C, ldc, sC, alpha, 1, K, 0);
+    LGB_CUDA(cudaGetLastError());
+    return LGB_OK;
+  }
+  const int kchunk = round_up(cdiv(K, splits), ZBK);
+  splits = cdiv(K, kchunk);
+  keep_pool_memory();
+  double2* P = nullptr;
+  LGB_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&P), (size_t)splits * sP * sizeof(double2), s));
+  dim3 grid(cdiv(N, ZBN), cdiv(M, ZBM), batch * splits);
+  zgemm_kernel<<<grid, 256, 0, s>>>(M, N, K, A, lda, sA, B, ldb, sB, P, N, (long long)M * N, 1.0,
+                                    splits, kchunk, sP);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    dim3 rgrid(cdiv(N, 128), M, batch);
+    zgemm_reduce_kernel<<<rgrid, 128, 0, s>>>(P, splits, sP, M, N, C, ldc, sC, alpha);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(P, s);
+  LGB_CUDA(e);
   return LGB_OK;
 }
 
