@@ -15,12 +15,17 @@
 //
 // Accumulation.  The tensor core's FP32 accumulate rounds toward zero on
 // every MMA, a bias that grows with the length of the accumulation chain
-// (measured: 1.8e-5 relative at K = 2048 with one chain per tile).  So every
-// 64-wide K block is its own short chain: its 12 MMAs (4 k-steps x 3 split
-// products) go into one of two TMEM accumulators, the small cross terms
-// hi.lo + lo.hi first and the dominant hi.hi last, so that only the last 4
-// MMAs round at full magnitude.  The epilogue warps fold each block into
-// round-to-nearest FP32 registers while the MMA fills the other accumulator.
+// (measured: 1.8e-5 relative at K = 2048 with one chain per tile).  So the
+// chains are short: with fp16 operands every 64-wide K block is its own chain
+// (12 MMAs: 4 k-steps x 3 split products, the small cross terms hi.lo + lo.hi
+// first and the dominant hi.hi last, so that only the last 4 MMAs round at
+// full magnitude); with bf16 operands two consecutive K blocks share one
+// chain, which halves the drains and lets the MMA run twice as far ahead
+// while the epilogue writes an item's output (+4.7 % on the broadband
+// workload; its error vs the complex128 plan goes from 3.5e-7 to 6.8e-7).
+// The chains alternate between two TMEM accumulators, and the epilogue warps
+// fold each into round-to-nearest FP32 registers while the MMA fills the
+// other one.
 //
 // CTA pairs (cta_group::2).  Two CTAs of a cluster run on a TPC's two SMs
 // and compute one 256 x 256 output tile together: CTA r holds rows
@@ -67,6 +72,13 @@ constexpr int EPI_WARPS = 8;
 constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
 constexpr uint32_t STG_BYTES = 4096;                       // output staging per epilogue warp
 constexpr unsigned long long WAIT_NS = 2000000000ull;      // 2 s bound on any wait
+// K blocks per accumulator drain: 2 for bf16 operands (the fast form: half
+// the drains, and twice the MMA run-ahead across an item's output pass), 1
+// for fp16 (the accurate form: the shortest round-toward-zero chains).
+template <bool BF16>
+struct Drain {
+  static constexpr int KB = BF16 ? 2 : 1;
+};
 
 // Pair-tile width: 256 output columns (the fast shape for large transforms:
 // each A tile feeds twice the MMA work) or 128 (twice the tiles, for launches
@@ -525,22 +537,25 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
   } else if (warp == 1) {
     // ------------------------------------------------------- MMA issuer
     if (leader && lane == 0) {
-      uint32_t it = 0;                       // K blocks issued (also accumulator uses)
+      uint32_t it = 0;                       // K blocks issued (stage ring)
+      uint32_t gi = 0;                       // accumulator groups issued (accumulator uses)
       bool ok = true;
       for (int i = pair; ok && i < p.n_items; i += npairs) {
         const uint32_t idesc = (p.idesc & ~(0x3Fu << 17)) |
                                ((uint32_t)(tile_n<BN>(p, decode(p, i).tn) >> 3) << 17);
         for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
-          const int s = it % STAGES, xb = it & 1;
+          const int s = it % STAGES, xb = gi & 1;
+          const bool first = kb % Drain<BF16>::KB == 0;
+          const bool last = kb % Drain<BF16>::KB == Drain<BF16>::KB - 1 || kb == p.kblocks - 1;
           if (!mbar_wait(full_bar(s), (it / STAGES) & 1, p.err)) { ok = false; break; }
-          // accumulator xb was drained by both CTAs (its previous block, it - 2)
-          if (!mbar_wait(acc_empty(xb), ((it >> 1) & 1) ^ 1, p.err)) { ok = false; break; }
+          // accumulator xb was drained by both CTAs (its previous group, gi - 2)
+          if (first && !mbar_wait(acc_empty(xb), ((gi >> 1) & 1) ^ 1, p.err)) { ok = false; break; }
           tc_fence_after();
           const uint32_t sa = base + s * STAGE_BYTES, X = tmem + xb * ACC_COLS;
 #pragma unroll
           for (int k = 0; k < KSTEPS; ++k) {     // hi.lo + lo.hi: small terms first
             mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + B_BYTES + k * 32),
-                    idesc, k ? 1u : 0u);
+                    idesc, (first && k == 0) ? 0u : 1u);
             mma_f16(X, smem_desc(sa + A_BYTES + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32),
                     idesc, 1u);
           }
@@ -548,7 +563,10 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
           for (int k = 0; k < KSTEPS; ++k)       // hi.hi last
             mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32), idesc, 1u);
           mma_commit_pair(empty_bar(s));         // both CTAs' stage s free once these retire
-          mma_commit_pair(acc_full(xb));         // accumulator xb ready for the epilogues
+          if (last) {
+            mma_commit_pair(acc_full(xb));       // accumulator xb ready for the epilogues
+            ++gi;
+          }
         }
       }
       // all issued MMAs have retired before TMEM is released
@@ -563,17 +581,18 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
     const uint32_t trow = tmem + ((uint32_t)(q4 * 32) << 16);
     const uint32_t empty_lead[2] = {map_to_cta(acc_empty(0), 0), map_to_cta(acc_empty(1), 0)};
     uint8_t* const stg = gbase + STAGES * STAGE_BYTES + (warp - 2) * STG_BYTES;
-    uint32_t it = 0;
+    uint32_t gi = 0;                         // accumulator groups drained
     bool ok = true;
+    const int groups = (p.kblocks + Drain<BF16>::KB - 1) / Drain<BF16>::KB;
     for (int i = pair; ok && i < p.n_items; i += npairs) {
       Item w = decode(p, i);
       w.tm = 2 * w.tm + (int)rank;           // this CTA's 128-row tile
       float run[C::RUN];
 #pragma unroll
       for (int j = 0; j < C::RUN; ++j) run[j] = 0.f;
-      for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
-        const int xb = it & 1;
-        ok = __all_sync(0xffffffffu, mbar_wait(acc_full(xb), (it >> 1) & 1, p.err));
+      for (int g = 0; g < groups; ++g, ++gi) {
+        const int xb = gi & 1;
+        ok = __all_sync(0xffffffffu, mbar_wait(acc_full(xb), (gi >> 1) & 1, p.err));
         if (!ok) break;
         tc_fence_after();
         drain_add<C::RUN>(trow + xb * ACC_COLS, p.stage, ch, run);
