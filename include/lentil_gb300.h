@@ -115,6 +115,10 @@ size_t lgb_dft2_plan_workspace_size(lgb_dft2_plan plan, int count);
 int lgb_dft2_plan_execute(lgb_dft2_plan plan, const lgb_c128* f, int count, lgb_c128* F,
                           void* workspace, size_t workspace_bytes, lgb_stream stream);
 int lgb_dft2_plan_status(lgb_dft2_plan plan, lgb_stream stream);
+/* Test hook for the status path: stores LGB_ETIMEOUT (or LGB_OK) into the
+ * plan's device status flag, stream-ordered, as an expired pipeline wait
+ * would; no kernel of the transform is involved. */
+int lgb_dft2_plan_inject_status(lgb_dft2_plan plan, int code, lgb_stream stream);
 int lgb_dft2_plan_destroy(lgb_dft2_plan plan);
 
 /* ------------------------------------------------------------------------

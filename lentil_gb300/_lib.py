@@ -73,6 +73,7 @@ SIGNATURES = {
     'lgb_dft2_plan_execute': (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_size_t,
                                       c_void_p]),
     'lgb_dft2_plan_status': (c_int, [c_void_p, c_void_p]),
+    'lgb_dft2_plan_inject_status': (c_int, [c_void_p, c_int, c_void_p]),
     'lgb_dft2_plan_destroy': (c_int, [c_void_p]),
     'lgb_tuner_set_mode': (c_int, [c_int]),
     'lgb_tuner_force_tile': (c_int, [c_int]),

@@ -43,6 +43,8 @@ struct PlanCarve {
   }
 };
 
+__global__ void store_int_kernel(int* dst, int v) { *dst = v; }
+
 __global__ void store_axes_kernel(PhaseAxis rows, PhaseAxis cols, PhaseAxis* dst, double* unit2) {
   dst[0] = rows;
   dst[1] = cols;
@@ -405,6 +407,15 @@ extern "C" int lgb_dft2_plan_status(lgb_dft2_plan P, lgb_stream stream) {
     LGB_CUDA(cudaMemsetAsync(P->err, 0, sizeof(int), s));
     return set_error(h, "device-side wait expired inside the tensor-core MFT");
   }
+  return LGB_OK;
+}
+
+extern "C" int lgb_dft2_plan_inject_status(lgb_dft2_plan P, int code, lgb_stream stream) {
+  LGB_REQUIRE(P, LGB_EINVAL, "dft2_plan_inject_status: null plan");
+  LGB_REQUIRE(code == LGB_OK || code == LGB_ETIMEOUT, LGB_EINVAL,
+              "dft2_plan_inject_status: only LGB_OK or LGB_ETIMEOUT can be injected");
+  store_int_kernel<<<1, 1, 0, as_stream(stream)>>>(P->err, code);
+  LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }
 

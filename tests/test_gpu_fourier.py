@@ -213,3 +213,35 @@ def test_cached_plan_replays_under_graph_capture(cuda_device, precision):
     torch.cuda.synchronize()
     assert torch.equal(out, ref)
     fourier.plan_status()
+
+
+def test_plan_status_is_reported_by_the_next_execute(cuda_device):
+    # an expired pipeline wait, made on the host side (the plan's status flag
+    # set through the test hook, no transform kernel involved): the next
+    # execute of the plan raises it without a host wait in between, the
+    # status then reads clean, and the plan transforms correctly again
+    from lentil_gb300 import _lib
+    fourier = lg.fourier
+    fourier.clear_plan_cache()
+    rng = np.random.default_rng(12)
+    f = torch.as_tensor(rng.standard_normal((1, 32, 32)) + 0j, device='cuda')
+    kw = dict(shape=(24, 24), precision='split-bf16')
+    for _ in range(2):                                   # the second call creates the plan
+        good = fourier.dft2_batch(f, 0.03, **kw)
+    (plan,) = list(fourier._plans.values())
+    _lib.call('lgb_dft2_plan_inject_status', plan._h, _lib.ETIMEOUT, lg._device.stream_ptr())
+    fourier.dft2_batch(f, 0.03, **kw)                    # copies the flag out behind an event
+    torch.cuda.synchronize()
+    with pytest.raises(_lib.DeviceTimeout):
+        fourier.dft2_batch(f, 0.03, **kw)                # finds it and raises
+    fourier.plan_status()                                # cleared
+    again = fourier.dft2_batch(f, 0.03, **kw)
+    torch.cuda.synchronize()                             # (tuner trials may change the width)
+    assert lo.peak_normalised_error(again.cpu().numpy(), good.cpu().numpy()) < 1e-12
+    _lib.call('lgb_dft2_plan_inject_status', plan._h, _lib.ETIMEOUT, lg._device.stream_ptr())
+    with pytest.raises(_lib.DeviceTimeout):
+        fourier.plan_status()                            # the waiting check reports at once
+    fourier.plan_status()
+    with pytest.raises(ValueError):
+        _lib.call('lgb_dft2_plan_inject_status', plan._h, 3, lg._device.stream_ptr())
+    fourier.clear_plan_cache()
