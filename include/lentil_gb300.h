@@ -396,6 +396,12 @@ void lgb_tuner_clear(void);
 int lgb_tuner_entries(void);
 int lgb_tuner_lookup(int m, int n, int M, int N, int count, int precision, int epilogue);
 int lgb_tuner_last_tile(void);
+/* Decided classes as rows of 9 ints (the class key -- bf16, m, n, M, N,
+ * epilogue, waves of stage 1, waves of stage 2 -- then the width), for a
+ * cache file: export writes up to max_rows rows and returns how many classes
+ * are decided; import adds rows as decided classes (widths 128 or 256). */
+int lgb_tuner_export(int* rows, int max_rows);
+int lgb_tuner_import(const int* rows, int n);
 
 #ifdef __cplusplus
 }

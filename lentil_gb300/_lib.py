@@ -81,6 +81,8 @@ SIGNATURES = {
     'lgb_tuner_entries': (c_int, []),
     'lgb_tuner_lookup': (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_int]),
     'lgb_tuner_last_tile': (c_int, []),
+    'lgb_tuner_export': (c_int, [c_void_p, c_int]),
+    'lgb_tuner_import': (c_int, [c_void_p, c_int]),
     'lgb_pixelate': (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_size_t,
                              c_void_p]),
     'lgb_ptt_normal_workspace_size': (c_size_t, [c_int]),

@@ -9,8 +9,20 @@
 #include <string>
 
 #include "../../include/lentil_gb300.h"
+#include <nvtx3/nvToolsExt.h>
 
 namespace lgb {
+
+// NVTX range over a C entry point: shows the library's calls on the
+// timeline of Nsight tools; inert (one branch) when no tool is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define LGB_RANGE(name) ::lgb::NvtxRange lgb_nvtx_range_(name)
+
 
 // ---------------------------------------------------------------------------
 // error reporting: every entry point returns an int status and records a

@@ -260,6 +260,7 @@ extern "C" int lgb_dft2_plan_create_in(int m, int n, int M, int N, double alpha_
                                        double offset_r, double offset_c, int unitary,
                                        int precision, void* memory, size_t memory_bytes,
                                        lgb_stream stream, lgb_dft2_plan* plan) {
+  LGB_RANGE("lgb_dft2_plan_create_in");
   LGB_REQUIRE(plan, LGB_EINVAL, "dft2_plan_create: null plan pointer");
   *plan = nullptr;
   lgb_dft2_plan_s* P = new lgb_dft2_plan_s();
@@ -286,6 +287,7 @@ extern "C" int lgb_dft2_plan_create(int m, int n, int M, int N, double alpha_r, 
                                     double shift_r, double shift_c, double offset_r,
                                     double offset_c, int unitary, int precision,
                                     lgb_stream stream, lgb_dft2_plan* plan) {
+  LGB_RANGE("lgb_dft2_plan_create");
   LGB_REQUIRE(plan, LGB_EINVAL, "dft2_plan_create: null plan pointer");
   *plan = nullptr;
   lgb_dft2_plan_s* P = new lgb_dft2_plan_s();
@@ -321,6 +323,7 @@ extern "C" size_t lgb_dft2_plan_workspace_size(lgb_dft2_plan P, int count) {
 
 extern "C" int lgb_dft2_plan_execute(lgb_dft2_plan P, const lgb_c128* f, int count, lgb_c128* F,
                                      void* workspace, size_t workspace_bytes, lgb_stream stream) {
+  LGB_RANGE("lgb_dft2_plan_execute");
   LGB_REQUIRE(P && f && F, LGB_EINVAL, "dft2_plan_execute: null argument");
   LGB_REQUIRE(count >= 1 && count <= 65535, LGB_EINVAL, "dft2_plan_execute: count outside 1..65535");
   LGB_REQUIRE(workspace && ((uintptr_t)workspace & 255) == 0, LGB_EWORKSPACE,

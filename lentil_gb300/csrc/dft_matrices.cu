@@ -112,6 +112,7 @@ int launch_e2_block_split(const PhaseAxis* d_axes, int L, int n, int N, int kp, 
 extern "C" int lgb_dft2_matrices(int m, int n, int M, int N, double alpha_r, double alpha_c,
                                  double shift_r, double shift_c, double offset_r,
                                  double offset_c, lgb_c128* E1, lgb_c128* E2, lgb_stream stream) {
+  LGB_RANGE("lgb_dft2_matrices");
   using namespace lgb;
   LGB_REQUIRE(m > 0 && n > 0 && M > 0 && N > 0, LGB_EINVAL, "dft2_matrices: sizes must be positive");
   LGB_REQUIRE(E1 && E2, LGB_EINVAL, "dft2_matrices: null output");

@@ -342,6 +342,7 @@ using namespace lgb;
 extern "C" int lgb_phasor(const double* amp, double amp_value, const double* mask,
                           const double* opd, double opd_value, int H, int W, int r0, int c0,
                           int m, int n, double wavelength, lgb_c128* out, lgb_stream stream) {
+  LGB_RANGE("lgb_phasor");
   LGB_REQUIRE(out, LGB_EINVAL, "phasor: null output");
   LGB_REQUIRE(m >= 0 && n >= 0 && r0 >= 0 && c0 >= 0, LGB_EINVAL, "phasor: negative slice");
   LGB_REQUIRE((!amp && !mask && !opd) || (r0 + m <= H && c0 + n <= W), LGB_EINVAL,
@@ -359,6 +360,7 @@ extern "C" int lgb_phasor(const double* amp, double amp_value, const double* mas
 extern "C" int lgb_field_insert(const lgb_c128* f, int fm, int fn, int64_t off_r, int64_t off_c,
                                 void* out, int om, int on, double weight, int intensity,
                                 lgb_stream stream) {
+  LGB_RANGE("lgb_field_insert");
   LGB_REQUIRE(f && out, LGB_EINVAL, "field_insert: null pointer");
   LGB_REQUIRE(fm > 0 && fn > 0 && om > 0 && on > 0, LGB_EINVAL, "field_insert: empty array");
   // lentil/field.py:259-299: upper-left corner of the shifted field in the
@@ -388,6 +390,7 @@ extern "C" int lgb_field_insert(const lgb_c128* f, int fm, int fn, int64_t off_r
 extern "C" int lgb_field_multiply(const lgb_c128* a, int lda, int ar0, int ac0,
                                   const lgb_c128* b, int ldb, int br0, int bc0, lgb_c128* out,
                                   int om, int on, lgb_stream stream) {
+  LGB_RANGE("lgb_field_multiply");
   LGB_REQUIRE(a && b && out, LGB_EINVAL, "field_multiply: null pointer");
   LGB_REQUIRE(om >= 0 && on >= 0, LGB_EINVAL, "field_multiply: negative shape");
   if (om == 0 || on == 0) return LGB_OK;
@@ -443,6 +446,7 @@ static int grid_for(size_t count) {
 }  // namespace lgb
 
 extern "C" int lgb_abs2(const lgb_c128* F, double* I, size_t count, lgb_stream stream) {
+  LGB_RANGE("lgb_abs2");
   LGB_REQUIRE(F && I, LGB_EINVAL, "abs2: null pointer");
   if (!count) return LGB_OK;
   abs2_kernel<<<grid_for(count), 256, 0, as_stream(stream)>>>(reinterpret_cast<const double2*>(F),
@@ -453,6 +457,7 @@ extern "C" int lgb_abs2(const lgb_c128* F, double* I, size_t count, lgb_stream s
 
 extern "C" int lgb_intensity_adjoint(const lgb_c128* F, const double* grad_I, lgb_c128* Hc,
                                      size_t count, lgb_stream stream) {
+  LGB_RANGE("lgb_intensity_adjoint");
   LGB_REQUIRE(F && grad_I && Hc, LGB_EINVAL, "intensity_adjoint: null pointer");
   if (!count) return LGB_OK;
   intensity_adjoint_kernel<<<grid_for(count), 256, 0, as_stream(stream)>>>(
@@ -464,6 +469,7 @@ extern "C" int lgb_intensity_adjoint(const lgb_c128* F, const double* grad_I, lg
 extern "C" int lgb_phasor_adjoint(const lgb_c128* q, const lgb_c128* f, int m, int n,
                                   double wavelength, double* grad_opd, int ld, int r0, int c0,
                                   lgb_stream stream) {
+  LGB_RANGE("lgb_phasor_adjoint");
   LGB_REQUIRE(q && f && grad_opd, LGB_EINVAL, "phasor_adjoint: null pointer");
   LGB_REQUIRE(wavelength != 0.0, LGB_EINVAL, "phasor_adjoint: wavelength must be nonzero");
   if (m <= 0 || n <= 0) return LGB_OK;

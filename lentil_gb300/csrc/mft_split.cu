@@ -1084,3 +1084,36 @@ extern "C" int lgb_tuner_lookup(int m, int n, int M, int N, int count, int preci
 }
 
 extern "C" int lgb_tuner_last_tile(void) { return tc::t_last_tile; }
+
+extern "C" int lgb_tuner_export(int* rows, int max_rows) {
+  tc::Tuner& T = tc::tuner();
+  std::lock_guard<std::mutex> lock(T.mu);
+  int n = 0;
+  for (const auto& kv : T.table) {
+    if (!kv.second.best) continue;
+    if (rows && n < max_rows) {
+      for (int j = 0; j < 8; ++j) rows[9 * n + j] = kv.first[j];
+      rows[9 * n + 8] = kv.second.best;
+    }
+    ++n;
+  }
+  return n;
+}
+
+extern "C" int lgb_tuner_import(const int* rows, int n) {
+  LGB_REQUIRE(n >= 0 && (rows || n == 0), LGB_EINVAL, "tuner_import: bad rows");
+  for (int i = 0; i < n; ++i)
+    LGB_REQUIRE(rows[9 * i + 8] == 128 || rows[9 * i + 8] == 256, LGB_EINVAL,
+                "tuner_import: a width is not 128 or 256");
+  tc::Tuner& T = tc::tuner();
+  std::lock_guard<std::mutex> lock(T.mu);
+  for (int i = 0; i < n; ++i) {
+    tc::TuneKey key;
+    for (int j = 0; j < 8; ++j) key[j] = rows[9 * i + j];
+    tc::TuneEntry& e = T.table[key];
+    tc::drop_trials(e);
+    e.trials = 0;
+    e.best = rows[9 * i + 8];
+  }
+  return LGB_OK;
+}

@@ -50,6 +50,7 @@ static int scratch_address(void** out) {
 extern "C" int lgb_dft2_noalloc(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int N,
                                 double alpha_r, double alpha_c, double shift_r, double shift_c,
                                 double offset_r, double offset_c, int unitary, lgb_stream stream) {
+  LGB_RANGE("lgb_dft2_noalloc");
   using namespace lgb;
   LGB_REQUIRE(m > 0 && n > 0 && M > 0 && N > 0, LGB_EINVAL, "dft2_noalloc: sizes must be positive");
   const size_t need = lgb_dft2_workspace_size(m, n, M, N, LGB_FP64);

@@ -610,6 +610,7 @@ extern "C" size_t lgb_pixel_workspace_size(int N, int oversample) {
 
 extern "C" int lgb_pixel(const double* img, int rows, int cols, int oversample, double* out,
                          void* workspace, size_t workspace_bytes, lgb_stream stream) {
+  LGB_RANGE("lgb_pixel");
   LGB_REQUIRE(img && out && workspace, LGB_EINVAL, "pixel: null pointer");
   LGB_REQUIRE(rows == cols, LGB_EINVAL, "pixel: the pixel MTF is defined for square images");
   LGB_REQUIRE(rows > 0 && oversample > 0, LGB_EINVAL, "pixel: sizes must be positive");
@@ -627,6 +628,7 @@ extern "C" int lgb_pixel(const double* img, int rows, int cols, int oversample, 
 
 extern "C" int lgb_pixelate(const double* img, int rows, int cols, int oversample, double* out,
                             void* workspace, size_t workspace_bytes, lgb_stream stream) {
+  LGB_RANGE("lgb_pixelate");
   LGB_REQUIRE(img && out && workspace, LGB_EINVAL, "pixelate: null pointer");
   LGB_REQUIRE(rows == cols, LGB_EINVAL, "pixelate: the pixel MTF is defined for square images");
   LGB_REQUIRE(rows > 0 && oversample > 0, LGB_EINVAL, "pixelate: sizes must be positive");
@@ -671,6 +673,7 @@ extern "C" int lgb_power_spectrum(const double* noise, const double* mask, int N
                                   double pixelscale, double rms, double half_power_freq,
                                   double exponent, double* out, void* workspace,
                                   size_t workspace_bytes, lgb_stream stream) {
+  LGB_RANGE("lgb_power_spectrum");
   LGB_REQUIRE(noise && mask && out && workspace, LGB_EINVAL, "power_spectrum: null pointer");
   LGB_REQUIRE(N > 0, LGB_EINVAL, "power_spectrum: size must be positive");
   LGB_REQUIRE(workspace_bytes >= lgb_power_spectrum_workspace_size(N), LGB_EWORKSPACE,

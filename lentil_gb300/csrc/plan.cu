@@ -103,6 +103,7 @@ extern "C" int lgb_dft2_batch(const lgb_c128* f, int count, int m, int n, lgb_c1
                               double shift_c, double offset_r, double offset_c, int unitary,
                               int precision, void* workspace, size_t workspace_bytes,
                               lgb_stream stream) {
+  LGB_RANGE("lgb_dft2_batch");
   int st = check_sizes(m, n, M, N);
   if (st) return st;
   LGB_REQUIRE(count >= 1 && count <= 65535, LGB_EINVAL, "dft2: count outside 1..65535");
@@ -178,6 +179,7 @@ extern "C" int lgb_dft2(const lgb_c128* f, int m, int n, lgb_c128* F, int M, int
                         double alpha_r, double alpha_c, double shift_r, double shift_c,
                         double offset_r, double offset_c, int unitary, int precision,
                         void* workspace, size_t workspace_bytes, lgb_stream stream) {
+  LGB_RANGE("lgb_dft2");
   return lgb_dft2_batch(f, 1, m, n, F, M, N, alpha_r, alpha_c, shift_r, shift_c, offset_r,
                         offset_c, unitary, precision, workspace, workspace_bytes, stream);
 }
@@ -197,6 +199,7 @@ extern "C" int lgb_idft2(const lgb_c128* F, int m, int n, lgb_c128* f, int M, in
                          double alpha_r, double alpha_c, double shift_r, double shift_c,
                          int unitary, int precision, void* workspace, size_t workspace_bytes,
                          lgb_stream stream) {
+  LGB_RANGE("lgb_idft2");
   // lentil/fourier.py:193-198: conj(dft2(conj(F))) / F.size.  The conjugated
   // input lives in the caller's output buffer when the shapes allow,
   // otherwise in the tail of the workspace.
@@ -334,6 +337,7 @@ static int prof_end(lgb_psf_plan_s* P, int slot, cudaStream_t s, cudaEvent_t* e)
 }
 
 extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan, lgb_stream stream) {
+  LGB_RANGE("lgb_psf_plan_create");
   LGB_REQUIRE(desc && plan, LGB_EINVAL, "psf_plan_create: null argument");
   const lgb_psf_desc& d = *desc;
   *plan = nullptr;
@@ -514,6 +518,7 @@ static int psf_execute_n(lgb_psf_plan P, int B, const int* lam_idx, int n_sel, c
 
 extern "C" int lgb_psf_execute(lgb_psf_plan P, const double* amp, const double* opd,
                                const double* weights, double* out, int accumulate, lgb_stream stream) {
+  LGB_RANGE("lgb_psf_execute");
   LGB_REQUIRE(P, LGB_EINVAL, "psf_execute: null plan");
   return psf_execute_n(P, P->d.batch, nullptr, 0, amp, opd, weights, out, accumulate, stream);
 }
@@ -521,6 +526,7 @@ extern "C" int lgb_psf_execute(lgb_psf_plan P, const double* amp, const double* 
 extern "C" int lgb_psf_execute_batch(lgb_psf_plan P, int count, const double* amp,
                                      const double* opd, const double* weights, double* out,
                                      int accumulate, lgb_stream stream) {
+  LGB_RANGE("lgb_psf_execute_batch");
   return psf_execute_n(P, count, nullptr, 0, amp, opd, weights, out, accumulate, stream);
 }
 
@@ -533,6 +539,7 @@ extern "C" int lgb_psf_execute_ws(lgb_psf_plan P, int count, const int* lam_idx,
                                   const double* amp, const double* opd, const double* weights,
                                   double* out, int accumulate, void* workspace,
                                   size_t workspace_bytes, lgb_stream stream) {
+  LGB_RANGE("lgb_psf_execute_ws");
   LGB_REQUIRE(P, LGB_EINVAL, "psf_execute_ws: null plan");
   LGB_REQUIRE(is_split(P->d.precision), LGB_EUNSUPPORTED,
               "psf_execute_ws: caller workspaces serve split-precision plans");
@@ -550,6 +557,7 @@ extern "C" int lgb_psf_execute_ws(lgb_psf_plan P, int count, const int* lam_idx,
 extern "C" int lgb_psf_execute_subset(lgb_psf_plan P, int count, const int* lam_idx, int n_sel,
                                       const double* amp, const double* opd, const double* weights,
                                       double* out, int accumulate, lgb_stream stream) {
+  LGB_RANGE("lgb_psf_execute_subset");
   LGB_REQUIRE(lam_idx, LGB_EINVAL, "psf_execute_subset: null wavelength index");
   return psf_execute_n(P, count, lam_idx, n_sel, amp, opd, weights, out, accumulate, stream);
 }

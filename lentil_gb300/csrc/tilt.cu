@@ -130,6 +130,7 @@ extern "C" size_t lgb_ptt_normal_workspace_size(int S) {
 extern "C" int lgb_ptt_normal(const double* opd, const double* mask, int S, int H, int W,
                               double ps_r, double ps_c, double* out, void* workspace,
                               size_t workspace_bytes, lgb_stream stream) {
+  LGB_RANGE("lgb_ptt_normal");
   LGB_REQUIRE(opd && mask && out, LGB_EINVAL, "ptt_normal: null pointer");
   LGB_REQUIRE(S > 0 && H > 0 && W > 0, LGB_EINVAL, "ptt_normal: sizes must be positive");
   LGB_REQUIRE(S <= 65535, LGB_EINVAL, "ptt_normal: too many masks");
@@ -147,6 +148,7 @@ extern "C" int lgb_ptt_normal(const double* opd, const double* mask, int S, int 
 extern "C" int lgb_remove_tilt(const double* opd, const double* mask, int S, int H, int W,
                                double ps_r, double ps_c, const double* t, double* out,
                                lgb_stream stream) {
+  LGB_RANGE("lgb_remove_tilt");
   LGB_REQUIRE(opd && mask && t && out, LGB_EINVAL, "remove_tilt: null pointer");
   LGB_REQUIRE(S > 0 && H > 0 && W > 0, LGB_EINVAL, "remove_tilt: sizes must be positive");
   const size_t total = (size_t)H * W;

@@ -125,6 +125,7 @@ extern "C" int lgb_zernike_coordinates(const double* mask, int H, int W, int aut
                                        double shift_r, double shift_c, double rotate, double* rho,
                                        double* theta, void* workspace, size_t workspace_bytes,
                                        lgb_stream stream) {
+  LGB_RANGE("lgb_zernike_coordinates");
   LGB_REQUIRE(mask && rho && theta, LGB_EINVAL, "zernike_coordinates: null pointer");
   LGB_REQUIRE(H > 0 && W > 0, LGB_EINVAL, "zernike_coordinates: sizes must be positive");
   LGB_REQUIRE(workspace && workspace_bytes >= lgb_zernike_workspace_size(), LGB_EWORKSPACE,
@@ -161,6 +162,7 @@ extern "C" int lgb_zernike_coordinates(const double* mask, int H, int W, int aut
 extern "C" int lgb_zernike_eval(const double* rho, const double* theta, const double* mask,
                                 size_t count, const double* table, int K, int T, double* out,
                                 int basis, lgb_stream stream) {
+  LGB_RANGE("lgb_zernike_eval");
   LGB_REQUIRE(rho && theta && mask && table && out, LGB_EINVAL, "zernike_eval: null pointer");
   LGB_REQUIRE(K > 0 && T > 0, LGB_EINVAL, "zernike_eval: empty mode table");
   if (count == 0) return LGB_OK;

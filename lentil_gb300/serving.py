@@ -24,7 +24,11 @@ weights, optics) are queued by any thread and scheduled by one GPU thread:
   cannot occupy every CTA pair;
 - a small launch shape seen twice keeps its buffers and is captured into a
   CUDA graph (one per tile width) that later launches replay;
-- completion is detected with CUDA events; latency is submit -> result.
+- completion is detected with CUDA events; latency is submit -> result;
+- a request whose plan cannot be built, or a launch whose buffers cannot be
+  allocated, fails with that exception while the server keeps serving; any
+  other error of the scheduling loop fails the queued requests instead of
+  leaving their futures waiting.
 """
 import collections
 import concurrent.futures
@@ -36,6 +40,7 @@ import torch
 
 from . import _device as dv
 from . import _lib
+from . import tuner
 from . import util
 from .broadband import make_plan, plan_geometry
 from .ptype import pupil as PUPIL
@@ -183,8 +188,11 @@ class PSFServer:
     SHARED_TILE = 256     # tile width of launches issued while others are in flight
 
     def __init__(self, hbm_budget=None, streams=4, max_batch=4, precision='split',
-                 use_graphs=True, grid=None, device=None):
+                 use_graphs=True, grid=None, device=None, tuner_cache=None):
         self.device = device or dv.device()
+        self.tuner_cache = tuner_cache       # tile widths loaded now, saved on close
+        if tuner_cache:
+            tuner.load(tuner_cache)
         free, total = torch.cuda.mem_get_info(self.device)
         # budget for resident plans; launch buffers come on top, from the
         # caching allocator, at most one launch per stream
@@ -196,6 +204,7 @@ class PSFServer:
         if precision == 'fp64':
             self.grid = np.zeros(0)                   # wavelength subsets need split plans
         self.n_streams = streams
+        self._alloc_failures = 0
         self._queue = collections.deque()
         self._cv = threading.Condition()
         self._slots = collections.OrderedDict()     # key -> _Slot, LRU order
@@ -222,6 +231,12 @@ class PSFServer:
             self._cv.notify()
         return req.future
 
+    def inject_allocation_failures(self, n):
+        """Test hook: the next ``n`` launch allocations fail on the host (as
+        ``torch.cuda.OutOfMemoryError``); their requests fail with it and the
+        server keeps serving."""
+        self._alloc_failures = int(n)
+
     def cancel(self, req):
         """Remove a queued (not yet launched) request; True if it was removed."""
         with self._cv:
@@ -239,6 +254,8 @@ class PSFServer:
             self._cv.notify()
         if wait:
             self._thread.join()
+        if self.tuner_cache:
+            tuner.save(self.tuner_cache)
 
     def __enter__(self):
         return self
@@ -271,8 +288,18 @@ class PSFServer:
         torch.cuda.set_device(self.device)
         self._streams = [torch.cuda.Stream(device=self.device) for _ in range(self.n_streams)]
         while True:
-            progressed = self._poll()
-            progressed |= self._admit()
+            try:
+                progressed = self._poll()
+                progressed |= self._admit()
+            except Exception as e:                   # never leave futures hanging
+                self.stats['loop_errors'] += 1
+                with self._cv:
+                    stuck = list(self._queue)
+                    self._queue.clear()
+                for r in stuck:
+                    if not r.future.done():
+                        r.future.set_exception(e)
+                progressed = True
             with self._cv:
                 if self._stop and not self._queue and not self._inflight:
                     return
@@ -353,7 +380,17 @@ class PSFServer:
                 break
             chosen = None
             for req in pending:                       # oldest request first
-                slot = self._slot_for(req)
+                try:
+                    slot = self._slot_for(req)
+                except (MemoryError, RuntimeError) as e:   # plan allocation or build failed
+                    with self._cv:
+                        if req in self._queue:
+                            self._queue.remove(req)
+                    req.t_done = time.perf_counter()
+                    req.future.set_exception(e)
+                    self.stats['failed'] += 1
+                    progressed = True
+                    continue
                 if isinstance(slot, str):             # 'too_big' or 'empty'
                     with self._cv:
                         self._queue.remove(req)
@@ -378,19 +415,36 @@ class PSFServer:
                 for r in batch:
                     self._queue.remove(r)
             n_sel = len(batch[0].wavelengths) if slot.grid else len(slot.geo.wavelengths)
-            b, reuse = slot.buffers(len(batch), n_sel, self.device, self.use_graphs)
-            hW = b.hW.view(len(batch), n_sel).numpy()
-            for k, r in enumerate(batch):
-                b.hA[k].numpy()[...] = r.amp
-                b.hO[k].numpy()[...] = r.opd
-                hW[k] = r.weights if slot.grid else r.weights[slot.geo.keep]
-            if slot.grid:
-                b.hlam.numpy()[...] = batch[0]._subset
             si = self._free_streams.pop(0)
-            b.busy = True
             slot.inflight += 1
-            tile = self.SHARED_TILE if self._inflight else 0
-            ev = slot.run(b, self._streams[si], reuse, tile)
+            b = None
+            try:
+                if self._alloc_failures > 0:         # test hook: the allocation fails
+                    self._alloc_failures -= 1
+                    raise torch.cuda.OutOfMemoryError('injected allocation failure')
+                b, reuse = slot.buffers(len(batch), n_sel, self.device, self.use_graphs)
+                hW = b.hW.view(len(batch), n_sel).numpy()
+                for k, r in enumerate(batch):
+                    b.hA[k].numpy()[...] = r.amp
+                    b.hO[k].numpy()[...] = r.opd
+                    hW[k] = r.weights if slot.grid else r.weights[slot.geo.keep]
+                if slot.grid:
+                    b.hlam.numpy()[...] = batch[0]._subset
+                b.busy = True
+                tile = self.SHARED_TILE if self._inflight else 0
+                ev = slot.run(b, self._streams[si], reuse, tile)
+            except (MemoryError, RuntimeError) as e:     # torch OOM is a RuntimeError
+                if b is not None:
+                    b.busy = False
+                slot.inflight -= 1
+                self._free_streams.append(si)
+                now = time.perf_counter()
+                for r in batch:
+                    r.t_done = now
+                    r.future.set_exception(e)
+                self.stats['failed'] += len(batch)
+                progressed = True
+                continue
             self._inflight.append((ev, slot, b, batch, si))
             self.stats['launches'] += 1
             self.stats['batched'] += len(batch)

@@ -13,6 +13,10 @@ and a later launch keeps the faster -- no relaunch, no host wait.  In
 include/lentil_gb300.h.
 """
 import contextlib
+import json
+import os
+
+import numpy as np
 
 from . import _lib
 
@@ -61,3 +65,41 @@ def lookup(m, n, M, N, count, precision='split', epilogue='intensity'):
 def last_tile():
     """Width used by this thread's last split launch (0 before any)."""
     return _lib.load().lgb_tuner_last_tile()
+
+
+def _device_tag():
+    import torch
+    p = torch.cuda.get_device_properties(torch.cuda.current_device())
+    return {'name': p.name, 'sm_count': int(p.multi_processor_count)}
+
+
+def save(path):
+    """Write the decided launch classes to a JSON cache file (atomically)."""
+    lib = _lib.load()
+    n = lib.lgb_tuner_export(None, 0)
+    rows = np.zeros((max(n, 1), 9), dtype=np.int32)
+    n = min(n, lib.lgb_tuner_export(rows.ctypes.data, rows.shape[0]))
+    doc = {'version': 1, 'device': _device_tag(), 'classes': rows[:n].tolist()}
+    tmp = f'{path}.tmp{os.getpid()}'
+    with open(tmp, 'w') as fh:
+        json.dump(doc, fh)
+    os.replace(tmp, path)
+    return n
+
+
+def load(path):
+    """Add the classes of a cache file written by ``save`` on the same kind of
+    GPU (same name and SM count: the classes are counted in waves over its
+    CTA pairs); returns how many were loaded (0 for a missing, foreign or
+    unreadable file)."""
+    try:
+        with open(path) as fh:
+            doc = json.load(fh)
+    except (OSError, ValueError):
+        return 0
+    if doc.get('version') != 1 or doc.get('device') != _device_tag():
+        return 0
+    rows = np.asarray(doc.get('classes', []), dtype=np.int32).reshape(-1, 9)
+    rows = np.ascontiguousarray(rows)
+    _lib.call('lgb_tuner_import', rows.ctypes.data, rows.shape[0])
+    return int(rows.shape[0])

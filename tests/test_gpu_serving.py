@@ -107,3 +107,22 @@ def test_grid_plans_serve_wavelength_subsets(cuda_device):
     assert stats['plans_built'] == 1
     for r, img in zip(reqs, out):
         assert lo.peak_normalised_error(img, _alone(r)) < TOL
+
+
+def test_allocation_failure_fails_only_its_launch(cuda_device):
+    # a launch whose buffers cannot be allocated (made on the host through the
+    # test hook) fails its requests with the allocation error; the server
+    # keeps its stream and slot accounting and serves the following requests
+    import torch
+    rng = np.random.default_rng(9)
+    with serving.PSFServer(streams=1, max_batch=1, precision='split') as srv:
+        srv.inject_allocation_failures(1)
+        first = _request(rng, 64, 16, 2)
+        with pytest.raises(torch.cuda.OutOfMemoryError):
+            srv.submit(first).result(timeout=120)
+        later = [_request(rng, 64, 16, 2) for _ in range(3)]
+        out = [srv.submit(r).result(timeout=120) for r in later]
+        stats = dict(srv.stats)
+    assert stats['failed'] == 1 and stats['completed'] == 3
+    for r, img in zip(later, out):
+        assert lo.peak_normalised_error(img, _alone(r)) < TOL

@@ -184,3 +184,31 @@ def test_tuner_argument_errors(cuda_device):
         tuner.force_tile(64)
     with pytest.raises(ValueError):
         tuner.set_mode('fastest')
+
+
+def test_tuner_cache_file_round_trip(cuda_device, tmp_path):
+    # decided classes survive a save / clear / load cycle; a file from another
+    # kind of GPU (or an unreadable one) is ignored
+    import json
+    tuner.clear()
+    tuner.set_mode('model')
+    rng = np.random.default_rng(13)
+    f = rng.standard_normal((2, 40, 30)) + 0j
+    lg.fourier.dft2_batch(f, 0.02, shape=(32, 36), precision='split-bf16')
+    w = tuner.lookup(40, 30, 32, 36, 2, 'split-bf16', 'complex')
+    assert w in (128, 256)
+    path = tmp_path / 'tiles.json'
+    assert tuner.save(str(path)) == tuner.entries() >= 1
+    tuner.clear()
+    assert tuner.lookup(40, 30, 32, 36, 2, 'split-bf16', 'complex') == 0
+    assert tuner.load(str(path)) >= 1
+    assert tuner.lookup(40, 30, 32, 36, 2, 'split-bf16', 'complex') == w
+    doc = json.loads(path.read_text())
+    doc['device']['sm_count'] += 1
+    other = tmp_path / 'other.json'
+    other.write_text(json.dumps(doc))
+    tuner.clear()
+    assert tuner.load(str(other)) == 0 and tuner.entries() == 0
+    (tmp_path / 'bad.json').write_text('{not json')
+    assert tuner.load(str(tmp_path / 'bad.json')) == 0
+    assert tuner.load(str(tmp_path / 'missing.json')) == 0
