@@ -50,6 +50,36 @@ class _ProbeWavefront:
         self.shape, self.data, self.ptype = shape, data, ptype
 
 
+class CapturedExecute:
+    """A PSFPlan execute captured as a CUDA graph (see ``PSFPlan.capture``)."""
+
+    def __init__(self, plan, amp, opd, weights, out, lam_idx=None):
+        self.plan, self.amp, self.opd, self.weights, self.out = plan, amp, opd, weights, out
+        self.lam_idx = lam_idx
+        count = int(amp.shape[0])
+        n_sel = None if lam_idx is None else int(lam_idx.numel())
+        self.ws = torch.empty(max(1, plan.workspace_bytes(count, n_sel)), dtype=torch.uint8,
+                              device=amp.device)
+        run = lambda: plan.execute(amp, opd, weights, out=out, check=False, lam_idx=lam_idx,
+                                   workspace=self.ws)
+        s = torch.cuda.Stream(device=amp.device)
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            run()                         # warm-up outside the capture (tuner, attributes)
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=s):
+                run()
+        torch.cuda.current_stream().wait_stream(s)
+
+    def replay(self):
+        """Rerun the captured execute on the current stream; returns ``out``."""
+        self.graph.replay()
+        return self.out
+
+    def status(self):
+        _lib.call('lgb_dft2_status', self.ws.data_ptr(), dv.stream_ptr())
+
+
 class PSFPlan:
     """Device plan for a batch of broadband PSFs with fixed optics.
 
@@ -104,6 +134,15 @@ class PSFPlan:
         """Pair-tile width of this plan's tensor-core launches: 0 = the
         autotuner's choice (``lentil_gb300.tuner``), 256 or 128 = that width."""
         _lib.call('lgb_psf_plan_set_tile', self._h, int(tile))
+
+    def capture(self, amp, opd, weights, out, lam_idx=None):
+        """The execute of these device tensors, captured once as a CUDA graph.
+
+        Returns a ``CapturedExecute`` whose ``replay()`` reruns it with
+        whatever the tensors hold at that moment (write new inputs into them in
+        place) and no host work per kernel; ``status()`` waits and raises a
+        device-side failure.  The plan must outlive the capture."""
+        return CapturedExecute(self, amp, opd, weights, out, lam_idx)
 
     def workspace_bytes(self, count, n_sel=None):
         """Bytes of a caller workspace for ``execute(..., workspace=...)``."""

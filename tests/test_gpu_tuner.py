@@ -212,3 +212,23 @@ def test_tuner_cache_file_round_trip(cuda_device, tmp_path):
     (tmp_path / 'bad.json').write_text('{not json')
     assert tuner.load(str(tmp_path / 'bad.json')) == 0
     assert tuner.load(str(tmp_path / 'missing.json')) == 0
+
+
+def test_captured_execute_replays_new_inputs(cuda_device):
+    # PSFPlan.capture: one CUDA graph of the execute; a replay after writing
+    # new inputs into the captured tensors equals a plain execute of them
+    plan, A, O, W = _small_plan('split-bf16', L=4, batch=2)
+    out = torch.empty((2, 80, 72), dtype=torch.float64, device='cuda')
+    cap = plan.capture(A, O, W, out)
+    first = cap.replay().clone()
+    torch.cuda.synchronize()
+    ref = plan.execute(A, O, W)
+    assert lo.peak_normalised_error(first.cpu().numpy(), ref.cpu().numpy()) < 1e-6
+    O.mul_(1.7)                                     # new inputs, in place
+    W[:, 0] = 0.0
+    got = cap.replay().clone()
+    cap.status()
+    ref2 = plan.execute(A, O, W)
+    for b in range(2):
+        assert lo.peak_normalised_error(got[b].cpu().numpy(), ref2[b].cpu().numpy()) < 1e-6
+    assert lo.peak_normalised_error(got[0].cpu().numpy(), first[0].cpu().numpy()) > 1e-3
