@@ -407,6 +407,29 @@ def run_gpu(args):
                 'kernel_ms_per_step': {name: kms[i] / args.steps
                                        for i, name in enumerate(_lib.PROFILE_SLOTS)}}
 
+    # ---------------- HBM rooflines of the elementwise kernels ---------------
+    # algorithmic bytes per launch: the phasor writes the split stage-1
+    # operand (hi + lo planes of f^T, n x 2 kp1 x 2 B each, per wavelength)
+    # after reading amp and opd over the field slice; the window add reads the
+    # FP32 window and read-modify-writes the float64 image
+    kp1 = (m + 31) // 32 * 32
+    hbm = pk.get('hbm_gbs', 6800.0)
+
+    def hbm_roofline(ms, nbytes, note=None):
+        gbs = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+        r = {'ms_per_launch': ms, 'algorithmic_bytes': nbytes, 'achieved_gbs': gbs,
+             'peak_gbs': hbm, 'frac': gbs / hbm, 'peak_kind': f'{pk_kind} HBM copy'}
+        if note:
+            r['note'] = note
+        return r
+
+    elementwise = {
+        'split_field_T_kernel': hbm_roofline(kms[0] / max(1, kcnt[0]),
+                                             (L * n * 2 * kp1 * 2 * 2 + 16 * m * n) * B),
+        'window_add_kernel': hbm_roofline(kms[3] / max(1, kcnt[3]), M * N * (4 + 16) * B,
+                                          'a 1024^2 window (20 MB) stays in the 129 MB L2'),
+    }
+
     # ---------------- CPU baseline (bounded sample) -------------------------
     cpu_s, idx = cpu_reference(wl, max(1, args.cpu_lambdas), opd[0])
     cpu_value = 1.0 / (cpu_s * len(wl.wavelengths))
@@ -430,6 +453,7 @@ def run_gpu(args):
                                                        'ms_per_psf': fp64_ms / B,
                                                        'speedup_split_over_fp64': value / world / fp64_value},
         'roofline': roofline,
+        'elementwise_roofline': elementwise,
         'cpu_baseline': {'value': cpu_value, 'unit': UNIT, 'cores': os.cpu_count(), 'kind': 'port',
                          'sample': f'{len(idx)} of {len(wl.wavelengths)} wavelengths of one PSF '
                                    'through lentil\'s per-segment user loop (numpy restatement '
@@ -710,6 +734,14 @@ def run_large(args):
     mean, p50, p99 = _timed(step, args.steps, args.warmup)
     img = step().cpu().numpy()
     res = {'split_ms': mean, 'p50_ms': p50, 'p99_ms': p99}
+    # pixelate alone (pixel MTF by FFT, then resampling): algorithmic bytes
+    # 2 x (8 B read + 8 B write) per input pixel plus the decimated write
+    pix_ms, _, _ = _timed(lambda: lg.detector.pixelate(out[0], wl.oversample), args.steps,
+                          args.warmup)
+    npx = out[0].numel()
+    pix_bytes = 32 * npx + 8 * npx // wl.oversample ** 2
+    pk, pk_kind = peaks()
+    pix_gbs = pix_bytes / (pix_ms / 1e3) / 1e9
     t1 = time.perf_counter()
     plan64 = broadband.make_plan(geo, batch=1, precision='fp64')
     ref = torch.zeros_like(out)
@@ -742,6 +774,11 @@ def run_large(args):
             'err_vs_fp64': err, 'fp64_plain': {'seconds_per_psf': fp64_s,
                                                'speedup_split_over_fp64': fp64_s * 1e3 / mean},
             'mft_tflops_algorithmic': flops / (mean / 1e3) / 1e12,
+            'pixelate_roofline': {'ms': pix_ms, 'algorithmic_bytes': pix_bytes,
+                                  'achieved_gbs': pix_gbs, 'peak_gbs': pk.get('hbm_gbs', 6800.0),
+                                  'frac': pix_gbs / pk.get('hbm_gbs', 6800.0),
+                                  'peak_kind': f'{pk_kind} HBM copy',
+                                  'path': 'detector.pixelate on the device image'},
             'input_prep_s': prep_s,
             'cpu_baseline': {'value': 1.0 / cpu_s, 'unit': 'PSFs/s', 'cores': os.cpu_count(),
                              'kind': 'port', 'sample': '1 of 32 wavelengths through the oracle '

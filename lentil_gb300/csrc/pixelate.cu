@@ -3,8 +3,11 @@
 // lentil applies the pixel MTF as |ifft2(fft2(img) * (s (x) s))| with
 // s[k] = sinc(fftfreq(N)[k] * os) (lentil/detector.py:218-222), for square
 // N x N images.  Two FP64 evaluations of that product:
-//   - N a power of two (<= 8192): the same FFT form, with this file's
-//     shared-memory radix-2 row FFTs and tiled transposes (~10 N^2 log2 N flop);
+//   - N a power of two (<= 8192): the product is separable, C . img . C^T
+//     with C = ifft diag(s) fft real and symmetric (s is real and even), so
+//     each axis is filtered by this file's shared-memory radix-2 FFTs with two
+//     real rows packed into one complex transform (fft, times s, inverse fft:
+//     C a + i C b), between tiled transposes (~5 N^2 log2 N flop);
 //   - any other N: |C . img . C^T| with C the real symmetric circulant
 //     C[i][j] = c[(i - j) mod N], c = ifft(s), as two FP64 GEMMs.
 // pixelate then resamples by 1/os with a cubic spline (lentil/util.py:261-349);
@@ -45,15 +48,10 @@ __global__ void real_to_complex_kernel(const double* __restrict__ x, double2* __
     z[p] = make_double2(x[p], 0.0);
 }
 
-// In-place FFT of every row (length N = 2^logN) in shared memory.
-__global__ void __launch_bounds__(512) fft_rows_kernel(double2* __restrict__ data, int N, int logN,
-                                                       const double2* __restrict__ tw,
-                                                       int inverse) {
-  extern __shared__ double2 sm[];
-  double2* row = data + (size_t)blockIdx.x * N;
-  for (int i = threadIdx.x; i < N; i += blockDim.x)
-    sm[__brev((unsigned)i) >> (32 - logN)] = row[i];
-  __syncthreads();
+// Radix-2 butterflies over a bit-reversed row in shared memory: natural
+// order out (the caller syncs before; this returns after a final sync).
+__device__ __forceinline__ void fft_stages(double2* sm, int N, int logN,
+                                           const double2* __restrict__ tw, int inverse) {
   for (int s = 1; s <= logN; ++s) {
     const int half = 1 << (s - 1);
     const int stride = N >> s;                         // twiddle index step
@@ -69,9 +67,76 @@ __global__ void __launch_bounds__(512) fft_rows_kernel(double2* __restrict__ dat
     }
     __syncthreads();
   }
+}
+
+// In-place FFT of every row (length N = 2^logN) in shared memory.
+__global__ void __launch_bounds__(512) fft_rows_kernel(double2* __restrict__ data, int N, int logN,
+                                                       const double2* __restrict__ tw,
+                                                       int inverse) {
+  extern __shared__ double2 sm[];
+  double2* row = data + (size_t)blockIdx.x * N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x)
+    sm[__brev((unsigned)i) >> (32 - logN)] = row[i];
+  __syncthreads();
+  fft_stages(sm, N, logN, tw, inverse);
   const double scale = inverse ? 1.0 / N : 1.0;
   for (int i = threadIdx.x; i < N; i += blockDim.x)
     row[i] = make_double2(sm[i].x * scale, sm[i].y * scale);
+}
+
+// The pixel MTF along rows: out_row = C . in_row with C = ifft diag(s) fft,
+// s = sinc(fftfreq(N) * os) real and even, so C is real.  Two real rows a, b
+// ride one complex transform z = a + i b: fft, times s, inverse fft gives
+// C a + i C b.  One block per row pair, one N-point buffer (the spectrum is
+// bit-reversed in place between the two transforms).
+__global__ void __launch_bounds__(512) pixel_filter_rows_kernel(const double* __restrict__ in,
+                                                                double* __restrict__ out, int N,
+                                                                int logN,
+                                                                const double2* __restrict__ tw,
+                                                                const double* __restrict__ sinc) {
+  extern __shared__ double2 sm[];
+  const size_t r0 = 2 * (size_t)blockIdx.x;
+  const double* ra = in + r0 * N;
+  const double* rb = ra + N;
+  const int shift = 32 - logN;
+  for (int i = threadIdx.x; i < N; i += blockDim.x)
+    sm[__brev((unsigned)i) >> shift] = make_double2(ra[i], rb[i]);
+  __syncthreads();
+  fft_stages(sm, N, logN, tw, 0);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double k = sinc[i];
+    sm[i] = make_double2(sm[i].x * k, sm[i].y * k);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {     // bit-reverse in place
+    const int j = (int)(__brev((unsigned)i) >> shift);
+    if (i < j) {
+      const double2 t = sm[i];
+      sm[i] = sm[j];
+      sm[j] = t;
+    }
+  }
+  __syncthreads();
+  fft_stages(sm, N, logN, tw, 1);
+  const double sc = 1.0 / N;
+  double* oa = out + r0 * N;
+  double* ob = oa + N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    oa[i] = sm[i].x * sc;
+    ob[i] = sm[i].y * sc;
+  }
+}
+
+// out = in^T (N x N float64), 32 x 32 tiles
+__global__ void transpose_f64_kernel(const double* __restrict__ in, double* __restrict__ out, int N) {
+  __shared__ double t[32][33];
+  const int x = blockIdx.x * 32 + threadIdx.x, y0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y)
+    if (x < N && y0 + k < N) t[k][threadIdx.x] = in[(size_t)(y0 + k) * N + x];
+  __syncthreads();
+  const int xo = blockIdx.y * 32 + threadIdx.x, yo0 = blockIdx.x * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y)
+    if (xo < N && yo0 + k < N) out[(size_t)(yo0 + k) * N + xo] = t[threadIdx.x][k];
 }
 
 // out = in^T (N x N complex128), 32 x 32 tiles
@@ -87,25 +152,22 @@ __global__ void transpose_c128_kernel(const double2* __restrict__ in, double2* _
     if (xo < N && yo0 + k < N) out[(size_t)(yo0 + k) * N + xo] = t[threadIdx.x][k];
 }
 
-// z[i][j] *= s[i] s[j]  (the separable pixel MTF; symmetric in i, j)
-__global__ void mtf_multiply_kernel(double2* __restrict__ z, int N, double os) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y;
-  if (j >= N) return;
-  const double k = sinc_os(i, N, os) * sinc_os(j, N, os);
-  double2 v = z[(size_t)i * N + j];
-  z[(size_t)i * N + j] = make_double2(v.x * k, v.y * k);
+// s[k] = sinc(fftfreq(N)[k] * os): N values, computed once per call (FP64
+// sinpi is slow on this part's FP64 pipe; the N^2 products below only read)
+__global__ void sinc_table_kernel(int N, double os, double* __restrict__ s) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < N) s[k] = sinc_os(k, N, os);
 }
 
 // ------------------------------------------------------------- GEMM path
 // c[k] = (1/N) sum_f s_f cos(2 pi f k / N)
-__global__ void pixel_taps_kernel(int N, double os, double* __restrict__ c) {
+__global__ void pixel_taps_kernel(int N, const double* __restrict__ sinc, double* __restrict__ c) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= N) return;
   double acc = 0.0;
   for (int f = 0; f < N; ++f) {
     const long long ph = ((long long)f * k) % N;         // exact phase index
-    acc += sinc_os(f, N, os) * cospi(2.0 * (double)ph / N);
+    acc += sinc[f] * cospi(2.0 * (double)ph / N);
   }
   c[k] = acc / N;
 }
@@ -381,13 +443,14 @@ static bool fft_size(int N, int* logN) {
 
 struct PixelSpace {
   double* sums;          // [0] sum p, [1] sum of the grid samples, [2] sum of the resampled
+  double* sinc;          // [N] sinc(fftfreq * os)
   double* d;
   // GEMM path
   double *c, *C, *T, *P;
   // FFT path
   double2 *X, *Y, *tw;
-  // off-grid resampling: |.| of the MTF product (FFT path), operator, passes
-  double *Pabs, *Gt, *Tm, *raw;
+  // off-grid resampling: operator and the two passes
+  double *Gt, *Tm, *raw;
   int* q0;
 };
 
@@ -404,6 +467,7 @@ static size_t pixel_space(void* ws, int N, int os, PixelSpace* s) {
   const size_t NN = (size_t)N * N;
   const int Nd = N / std::max(os, 1);
   t.sums = static_cast<double*>(take(4 * sizeof(double)));
+  t.sinc = static_cast<double*>(take((size_t)N * sizeof(double)));
   t.d = static_cast<double*>(take((size_t)Nd * Nd * sizeof(double)));
   const bool fft = fft_size(N, &logN);
   if (fft) {
@@ -418,8 +482,6 @@ static size_t pixel_space(void* ws, int N, int os, PixelSpace* s) {
   }
   const int S = resample_size(N, std::max(os, 1));
   if (!resample_on_grid(N, std::max(os, 1), S)) {
-    // decided by the path, not by a pointer: the size query carves from null
-    if (fft) t.Pabs = static_cast<double*>(take(NN * sizeof(double)));
     t.Gt = static_cast<double*>(take((size_t)RS_BW * S * sizeof(double)));
     t.q0 = static_cast<int*>(take((size_t)S * sizeof(int)));
     t.Tm = static_cast<double*>(take((size_t)N * S * sizeof(double)));
@@ -434,30 +496,32 @@ static int run_pixel(const double* img, int N, int os, void* ws, cudaStream_t s,
                      const void** src, bool* is_complex) {
   pixel_space(ws, N, os, w);
   LGB_CUDA(cudaMemsetAsync(w->sums, 0, 4 * sizeof(double), s));
+  sinc_table_kernel<<<cdiv(N, 256), 256, 0, s>>>(N, (double)os, w->sinc);
   int logN;
   if (fft_size(N, &logN)) {
-    const size_t NN = (size_t)N * N;
-    const int blocks = std::max(1, std::min(4 * sm_count(), (int)((NN + 255) / 256)));
+    // separable filter P = C . img . C^T (C real symmetric): filter the rows,
+    // transpose, filter the rows again, transpose back; X and Y hold the real
+    // N x N intermediates
+    double* R = reinterpret_cast<double*>(w->X);
+    double* RT = reinterpret_cast<double*>(w->Y);
     twiddle_kernel<<<cdiv(std::max(N / 2, 1), 256), 256, 0, s>>>(N, w->tw);
-    real_to_complex_kernel<<<blocks, 256, 0, s>>>(img, w->X, NN);
     const size_t smem = (size_t)N * sizeof(double2);
-    LGB_CUDA(cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    LGB_CUDA(cudaFuncSetAttribute(pixel_filter_rows_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   8192 * (int)sizeof(double2)));
     const int threads = std::min(512, std::max(32, N / 2));
     const dim3 tgrid(cdiv(N, 32), cdiv(N, 32)), tblock(32, 8);
-    fft_rows_kernel<<<N, threads, smem, s>>>(w->X, N, logN, w->tw, 0);       // rows
-    transpose_c128_kernel<<<tgrid, tblock, 0, s>>>(w->X, w->Y, N);
-    fft_rows_kernel<<<N, threads, smem, s>>>(w->Y, N, logN, w->tw, 0);       // columns
-    mtf_multiply_kernel<<<dim3(cdiv(N, 128), N), 128, 0, s>>>(w->Y, N, (double)os);
-    fft_rows_kernel<<<N, threads, smem, s>>>(w->Y, N, logN, w->tw, 1);
-    transpose_c128_kernel<<<tgrid, tblock, 0, s>>>(w->Y, w->X, N);
-    fft_rows_kernel<<<N, threads, smem, s>>>(w->X, N, logN, w->tw, 1);
+    pixel_filter_rows_kernel<<<N / 2, threads, smem, s>>>(img, R, N, logN, w->tw, w->sinc);
+    transpose_f64_kernel<<<tgrid, tblock, 0, s>>>(R, RT, N);
+    pixel_filter_rows_kernel<<<N / 2, threads, smem, s>>>(RT, R, N, logN, w->tw, w->sinc);
+    transpose_f64_kernel<<<tgrid, tblock, 0, s>>>(R, RT, N);
     LGB_CUDA(cudaGetLastError());
-    *src = w->X;
-    *is_complex = true;
+    w->P = RT;
+    *src = RT;
+    *is_complex = false;
     return LGB_OK;
   }
-  pixel_taps_kernel<<<cdiv(N, 128), 128, 0, s>>>(N, (double)os, w->c);
+  pixel_taps_kernel<<<cdiv(N, 128), 128, 0, s>>>(N, w->sinc, w->c);
   circulant_kernel<<<dim3(cdiv(N, 128), N), 128, 0, s>>>(N, w->c, w->C);
   dim3 grid(cdiv(N, DBN), cdiv(N, DBM));
   dgemm_kernel<<<grid, 256, 0, s>>>(N, w->C, img, w->T);      // T = C . img
@@ -647,7 +711,7 @@ extern "C" int lgb_pixelate(const double* img, int rows, int cols, int oversampl
     LGB_CUDA(cudaGetLastError());
     return LGB_OK;
   }
-  double* P = cplx ? w.Pabs : w.P;
+  double* P = w.P;                       // the real MTF product, made |.| in place
   if ((st = abs_reduce(N, 1, src, cplx, P, nullptr, w.sums, s))) return st;
   resample_operator_kernel<<<cdiv(S * RS_BW, 256), 256, 0, s>>>(N, os, S, w.Gt, w.q0);
   resample_rows_kernel<<<dim3(cdiv(S, 64), cdiv(N, 4 * RS_ROWS)), dim3(64, 4), 0, s>>>(

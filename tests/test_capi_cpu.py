@@ -70,13 +70,12 @@ def test_workspace_sizes_are_consistent(lib):
 @pytest.mark.parametrize('n,os_', [(2048, 3), (1000, 3), (64, 5), (75, 2), (5, 2)])
 def test_pixel_workspace_covers_off_grid_buffers(lib, n, os_):
     # the size query must count every buffer the off-grid pixelate carves:
-    # the MTF product (two complex planes on the FFT path, three real
-    # planes on the GEMM path), |p| (FFT path), the banded operator, both
-    # resampling passes
+    # the MTF product (two N x N planes on the FFT path, three real planes on
+    # the GEMM path), the banded operator, both resampling passes
     S = lib.lgb_pixelate_size(n, os_)
     assert S == int(np.ceil(n * (1 / os_)))
     fft = n >= 2 and n & (n - 1) == 0
-    need = (2 * 16 + 8) * n * n if fft else 3 * 8 * n * n
+    need = 2 * 8 * n * n if fft else 3 * 8 * n * n
     need += 8 * (64 * S + n * S + S * S) + 4 * S
     assert lib.lgb_pixel_workspace_size(n, os_) >= need
     assert lib.lgb_pixelate_size(0, 2) == -1 and lib.lgb_pixelate_size(10, 0) == -1
