@@ -131,4 +131,26 @@ template <> struct Split16<false> {
   }
 };
 
+// Two values at once, packed as two 16-bit lanes (x0 in the low half, x1 in
+// the high half) with paired conversions; each lane equals Split16::split.
+template <bool BF16> struct Split16x2;
+template <> struct Split16x2<true> {
+  static __device__ __forceinline__ void split(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    const float2 hf = __bfloat1622float2(h);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+  }
+};
+template <> struct Split16x2<false> {
+  static __device__ __forceinline__ void split(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+    const __half2 h = __floats2half2_rn(x0, x1);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(x0 - hf.x, x1 - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+  }
+};
+
 }  // namespace lgb

@@ -129,16 +129,9 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
     }
     uint32_t pk[4][4];                               // [plane][pair of rows]
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      uint16_t rh0, rl0, ih0, il0, rh1, rl1, ih1, il1;
-      Split16<BF16>::split(fv[2 * j].x, rh0, rl0);
-      Split16<BF16>::split(fv[2 * j].y, ih0, il0);
-      Split16<BF16>::split(fv[2 * j + 1].x, rh1, rl1);
-      Split16<BF16>::split(fv[2 * j + 1].y, ih1, il1);
-      pk[0][j] = (uint32_t)rh0 | ((uint32_t)rh1 << 16);
-      pk[1][j] = (uint32_t)rl0 | ((uint32_t)rl1 << 16);
-      pk[2][j] = (uint32_t)ih0 | ((uint32_t)ih1 << 16);
-      pk[3][j] = (uint32_t)il0 | ((uint32_t)il1 << 16);
+    for (int j = 0; j < 4; ++j) {                    // rows 2j, 2j+1 split as a pair
+      Split16x2<BF16>::split(fv[2 * j].x, fv[2 * j + 1].x, pk[0][j], pk[1][j]);
+      Split16x2<BF16>::split(fv[2 * j].y, fv[2 * j + 1].y, pk[2][j], pk[3][j]);
     }
     // buffer l&1 was last read two wavelengths ago, before the barrier of the
     // previous wavelength; row pitch 144 B keeps 8 lanes' 16-byte stores on

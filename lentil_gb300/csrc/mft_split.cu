@@ -379,11 +379,7 @@ __device__ __forceinline__ void write_stage1(const Params& p, const Item& w, int
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int k = cc * 32 + v8 * 8 + 2 * j;
-        uint16_t h0, l0, h1, l1;
-        Split16<BF16>::split(run[k] * p.sG, h0, l0);
-        Split16<BF16>::split(run[k + 1] * p.sG, h1, l1);
-        ph[j] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-        pl[j] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        Split16x2<BF16>::split(run[k] * p.sG, run[k + 1] * p.sG, ph[j], pl[j]);
       }
       const uint32_t slot = lane * 64 + ((v8 ^ ((lane >> 1) & 3)) << 4);
       *reinterpret_cast<uint4*>(stg + slot) = make_uint4(ph[0], ph[1], ph[2], ph[3]);
