@@ -126,3 +126,22 @@ def test_allocation_failure_fails_only_its_launch(cuda_device):
     assert stats['failed'] == 1 and stats['completed'] == 3
     for r, img in zip(later, out):
         assert lo.peak_normalised_error(img, _alone(r)) < TOL
+
+
+def test_server_tuner_cache_file(cuda_device, tmp_path):
+    # PSFServer(tuner_cache=path) writes the tile widths it decided on close
+    # and a later server loads them
+    import json
+    from lentil_gb300 import tuner
+    path = tmp_path / 'tiles.json'
+    rng = np.random.default_rng(10)
+    tuner.clear()
+    with serving.PSFServer(streams=1, max_batch=1, precision='split', tuner_cache=str(path)) as srv:
+        for _ in range(6):                  # one launch class, tuned while the GPU is idle
+            srv.submit(_request(rng, 64, 16, 2)).result(timeout=120)
+        decided = tuner.entries()
+    doc = json.loads(path.read_text())
+    assert len(doc['classes']) == decided >= 1
+    tuner.clear()
+    with serving.PSFServer(streams=1, max_batch=1, precision='split', tuner_cache=str(path)):
+        assert tuner.entries() == decided
