@@ -150,10 +150,12 @@ def plan_cache_info():
 
 
 def clear_plan_cache():
-    """Destroy every cached dft2 plan and forget the geometries seen once."""
+    """Destroy every cached dft2 plan that no captured CUDA graph holds (see
+    ``pinned_plans``) and forget the geometries seen once."""
     with _plans_lock:
-        while _plans:
-            _plans.popitem(last=False)[1].destroy()
+        for k in list(_plans):
+            if not _plans[k].pins:
+                _plans.pop(k).destroy()
         _seen.clear()
 
 

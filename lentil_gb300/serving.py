@@ -23,7 +23,8 @@ weights, optics) are queued by any thread and scheduled by one GPU thread:
   (``lentil_gb300.tuner``), which may be the narrower tile when it alone
   cannot occupy every CTA pair;
 - a small launch shape seen twice keeps its buffers and is captured into a
-  CUDA graph (one per tile width) that later launches replay;
+  CUDA graph (one per tile width; for the tuned width only once the tuner has
+  decided the launch class) that later launches replay;
 - completion is detected with CUDA events; latency is submit -> result;
 - a request whose plan cannot be built, or a launch whose buffers cannot be
   allocated, fails with that exception while the server keeps serving; any
@@ -132,6 +133,7 @@ class _Slot:
 
     def __init__(self, key, geo, precision, grid):
         self.key, self.geo, self.grid = key, geo, grid
+        self.precision = precision
         self.plan = make_plan(geo, batch=0, precision=precision)
         self.bytes = self.plan.nbytes
         self.static = {}              # (n, n_sel) -> _Buffers reused across launches
@@ -151,6 +153,15 @@ class _Slot:
             return b, True
         return b, False
 
+    def tile_decided(self, b):
+        """Whether the autotuner has settled the tile width of this launch's
+        class (a graph captured before that would keep the model's width)."""
+        if self.precision == 'fp64':
+            return True
+        m, n = self.geo.fslice[2], self.geo.fslice[3]
+        M, N = self.geo.window_shape
+        return tuner.lookup(m, n, M, N, b.n * b.n_sel, self.precision, 'intensity') != 0
+
     def run(self, b, stream, reuse, tile):
         """Launch buffers ``b`` (host inputs already staged) on ``stream``
         with pair-tile width ``tile`` (0: the autotuner's)."""
@@ -163,7 +174,7 @@ class _Slot:
             if self.grid:
                 b.lam.copy_(b.hlam, non_blocking=True)
             g = b.graphs.get(tile)
-            if reuse and g is None:
+            if reuse and g is None and (tile != 0 or self.tile_decided(b)):
                 b.launch(self)                       # warm-up outside capture
                 g = torch.cuda.CUDAGraph()
                 with torch.cuda.graph(g, stream=stream):

@@ -190,5 +190,12 @@ def test_graphed_loss_matches_eager(cuda_device, precision):
         assert torch.allclose(g2, c.grad, rtol=1e-10, atol=1e-12 * g2.abs().max().item())
     finally:
         lg.fourier.PLAN_CACHE_ENTRIES = old
+    lg.fourier.clear_plan_cache()               # pinned plans survive a clear
+    assert lg.fourier.plan_cache_info()[0] == n_pinned
+    c.grad = None
+    pr.graphed_loss(c).backward()
+    assert torch.isfinite(c.grad).all()
     pr.check()
     pr.release_graphs()
+    lg.fourier.clear_plan_cache()
+    assert lg.fourier.plan_cache_info()[0] == 0
