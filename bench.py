@@ -106,7 +106,9 @@ def run_reference(args):
     # the same seeded workload, its Zernike modes evaluated on the host
     wl = workloads.broadband_segmented(args.npix, args.wavelengths, basis=lo.zernike_basis)
     opd = wl.opds(1)[0]
-    n = max(1, args.cpu_lambdas)
+    # a bounded sample per step: --cpu-lambdas wavelengths, one when many
+    # steps are asked for, so that the whole run stays within minutes
+    n = max(1, args.cpu_lambdas) if args.steps <= 50 else 1
     for _ in range(args.warmup if args.warmup < 1 else 1):
         cpu_reference(wl, 1, opd)
     per = []
