@@ -280,6 +280,13 @@ int lgb_intensity_adjoint(const lgb_c128* F, const double* grad_I, lgb_c128* Hc,
                           lgb_stream stream);
 int lgb_phasor_adjoint(const lgb_c128* q, const lgb_c128* f, int m, int n, double wavelength,
                        double* grad_opd, int ld, int r0, int c0, lgb_stream stream);
+/* K phasors amp * exp(2 pi i opd[k] / wavelength) over the slice (r0, c0,
+ * m, n) of H x W planes, out[K][m][n], in one launch.  fast != 0 evaluates
+ * the phase in float-float and the sine in FP32 (about 1e-7 relative, for
+ * the split-precision transforms); fast == 0 matches lgb_phasor. */
+int lgb_phasor_stack(const double* amp, const double* opd, int K, int H, int W, int r0, int c0,
+                     int m, int n, double wavelength, int fast, lgb_c128* out,
+                     lgb_stream stream);
 
 /* ------------------------------------------------------------------------
  * Broadband PSF plan: the documented user loop

@@ -74,6 +74,8 @@ SIGNATURES = {
                                       c_void_p]),
     'lgb_dft2_plan_status': (c_int, [c_void_p, c_void_p]),
     'lgb_dft2_plan_inject_status': (c_int, [c_void_p, c_int, c_void_p]),
+    'lgb_phasor_stack': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int,
+                                 c_int, c_double, c_int, c_void_p, c_void_p]),
     'lgb_dft2_plan_destroy': (c_int, [c_void_p]),
     'lgb_tuner_set_mode': (c_int, [c_int]),
     'lgb_tuner_force_tile': (c_int, [c_int]),

@@ -42,19 +42,23 @@ def geometry(amp, wavelength, pixelscale_in, focal_length, pixelscale_out, shape
                     (r0, c0, m, n), tuple(a.shape), precision)
 
 
-def _phasor(amp, opd, g):
+def _phasor_stack(amp, opd, g):
+    """Fields f [K, m, n] of a stack opd [K, H, W] in one launch; the split
+    precisions take the FP32-sine form, whose 1e-7 error is below the 16-bit
+    operand split that follows."""
     r0, c0, m, n = g.slc
     H, W = g.plane
-    f = torch.empty((m, n), dtype=torch.complex128, device=amp.device)
-    _lib.call('lgb_phasor', amp.data_ptr(), 0.0, None, opd.data_ptr(), 0.0, H, W, r0, c0, m, n,
-              g.wavelength, f.data_ptr(), dv.stream_ptr())
+    K = int(opd.shape[0])
+    f = torch.empty((K, m, n), dtype=torch.complex128, device=amp.device)
+    _lib.call('lgb_phasor_stack', amp.data_ptr(), opd.data_ptr(), K, H, W, r0, c0, m, n,
+              g.wavelength, int(g.precision != 'fp64'), f.data_ptr(), dv.stream_ptr())
     return f
 
 
 def _forward_field(amp, opd, g):
     """Fields f [K, m, n] of a stack of OPD maps opd [K, H, W] and their
     transforms F [K, M, N] (one batched MFT for the whole stack)."""
-    f = torch.stack([_phasor(amp, o, g) for o in opd])
+    f = _phasor_stack(amp, opd.contiguous(), g)
     F = fourier.dft2_batch(f, g.alpha, shape=g.shape, shift=g.shift, offset=g.offset,
                            unitary=True, precision=g.precision)
     return f, F

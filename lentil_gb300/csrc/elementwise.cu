@@ -31,6 +31,40 @@ __global__ void phasor_c128_kernel(const double* __restrict__ amp, double amp_va
   out[(size_t)i * n + j] = make_double2(a * c, a * s);
 }
 
+// A stack of K phasors amp * exp(2 pi i opd_k / lambda) over one slice, for
+// the gradient path.  FAST: the phase as a float-float product opd * 2/lambda
+// reduced mod 2 half-cycles, then FP32 sincospi (about 1e-7 relative: for
+// operands that are rounded to 16-bit hi/lo planes next); otherwise FP64
+// sincospi as lgb_phasor.
+template <bool FAST>
+__global__ void phasor_stack_kernel(const double* __restrict__ amp,
+                                    const double* __restrict__ opd, int H, int W, int r0, int c0,
+                                    int m, int n, double two_over_lambda, float2 khalf,
+                                    double2* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  const int k = blockIdx.z;
+  if (j >= n || i >= m) return;
+  const size_t p = (size_t)(r0 + i) * W + (c0 + j);
+  const double a = amp[p];
+  const double o = opd[(size_t)k * H * W + p];
+  double s, c;
+  if (FAST) {
+    const float oh = (float)o, ol = (float)(o - (double)oh);
+    const float ph = oh * khalf.x;
+    float e = fmaf(oh, khalf.x, -ph);
+    e = fmaf(oh, khalf.y, fmaf(ol, khalf.x, e));
+    const float x = (ph - 2.f * rintf(0.5f * ph)) + e;
+    float sf, cf;
+    sincospif(x, &sf, &cf);
+    s = sf;
+    c = cf;
+  } else {
+    sincospi(o * two_over_lambda, &s, &c);
+  }
+  out[((size_t)k * m + i) * n + j] = make_double2(a * c, a * s);
+}
+
 __global__ void phasor_batch_c128_kernel(const double* __restrict__ amp,
                                          const double* __restrict__ opd, int H, int W, int r0,
                                          int c0, int m, int n,
@@ -331,6 +365,28 @@ __global__ void multiply_kernel(const double2* __restrict__ a, int lda, int ar0,
 }  // namespace lgb
 
 using namespace lgb;
+
+extern "C" int lgb_phasor_stack(const double* amp, const double* opd, int K, int H, int W,
+                                int r0, int c0, int m, int n, double wavelength, int fast,
+                                lgb_c128* out, lgb_stream stream) {
+  LGB_RANGE("lgb_phasor_stack");
+  LGB_REQUIRE(amp && opd && out, LGB_EINVAL, "phasor_stack: null pointer");
+  LGB_REQUIRE(K > 0 && K <= 65535 && m > 0 && n > 0 && r0 >= 0 && c0 >= 0 && r0 + m <= H &&
+                  c0 + n <= W, LGB_EINVAL, "phasor_stack: slice outside the plane");
+  LGB_REQUIRE(wavelength > 0, LGB_EINVAL, "phasor_stack: wavelength must be positive");
+  const double tol = 2.0 / wavelength;
+  const float hi = (float)tol;
+  const float2 kh = make_float2(hi, (float)(tol - (double)hi));
+  dim3 grid(cdiv(n, 128), m, K);
+  if (fast)
+    phasor_stack_kernel<true><<<grid, 128, 0, as_stream(stream)>>>(
+        amp, opd, H, W, r0, c0, m, n, tol, kh, reinterpret_cast<double2*>(out));
+  else
+    phasor_stack_kernel<false><<<grid, 128, 0, as_stream(stream)>>>(
+        amp, opd, H, W, r0, c0, m, n, tol, kh, reinterpret_cast<double2*>(out));
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
 
 extern "C" int lgb_phasor(const double* amp, double amp_value, const double* mask,
                           const double* opd, double opd_value, int H, int W, int r0, int c0,

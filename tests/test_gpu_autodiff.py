@@ -199,3 +199,26 @@ def test_graphed_loss_matches_eager(cuda_device, precision):
     pr.release_graphs()
     lg.fourier.clear_plan_cache()
     assert lg.fourier.plan_cache_info()[0] == 0
+
+
+def test_phasor_stack_forms(cuda_device):
+    # the exact form equals lgb_phasor bitwise; the FP32-sine form used by
+    # the split precisions stays within 1e-6 of it (large OPDs included)
+    from lentil_gb300 import _lib
+    rng = np.random.default_rng(14)
+    H, W, K, r0, c0, m, n = 40, 36, 3, 2, 3, 31, 29
+    amp = torch.as_tensor(rng.uniform(0, 1, (H, W)), device='cuda')
+    opd = torch.as_tensor(rng.normal(0, 2e-6, (K, H, W)), device='cuda')
+    s = torch.cuda.current_stream().cuda_stream
+    out = {}
+    for fast in (0, 1):
+        f = torch.empty((K, m, n), dtype=torch.complex128, device='cuda')
+        _lib.call('lgb_phasor_stack', amp.data_ptr(), opd.data_ptr(), K, H, W, r0, c0, m, n,
+                  633e-9, fast, f.data_ptr(), s)
+        out[fast] = f
+    for k in range(K):
+        one = torch.empty((m, n), dtype=torch.complex128, device='cuda')
+        _lib.call('lgb_phasor', amp.data_ptr(), 0.0, None, opd[k].data_ptr(), 0.0, H, W, r0, c0,
+                  m, n, 633e-9, one.data_ptr(), s)
+        assert torch.equal(out[0][k], one)
+    assert (out[1] - out[0]).abs().max().item() < 1e-6 * amp.max().item()
