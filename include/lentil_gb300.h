@@ -280,6 +280,15 @@ int lgb_intensity_adjoint(const lgb_c128* F, const double* grad_I, lgb_c128* Hc,
                           lgb_stream stream);
 int lgb_phasor_adjoint(const lgb_c128* q, const lgb_c128* f, int m, int n, double wavelength,
                        double* grad_opd, int ld, int r0, int c0, lgb_stream stream);
+/* Modal OPD for phase retrieval: out[p] = sum_k coeffs[k] basis[k][p] and
+ * its adjoint out[k] = sum_p basis[k][p] grad[p] (deterministic sums), with
+ * an FP32 basis [K][P] (K <= 1024): both stream the basis once.  Workspace of
+ * the adjoint: lgb_basis_project_workspace_size(K) bytes. */
+int lgb_basis_expand(const float* basis, const double* coeffs, int K, size_t P, double* out,
+                     lgb_stream stream);
+size_t lgb_basis_project_workspace_size(int K);
+int lgb_basis_project(const float* basis, const double* grad, int K, size_t P, double* out,
+                      void* workspace, size_t workspace_bytes, lgb_stream stream);
 /* K phasors amp * exp(2 pi i opd[k] / wavelength) over the slice (r0, c0,
  * m, n) of H x W planes, out[K][m][n], in one launch.  fast != 0 evaluates
  * the phase in float-float and the sine in FP32 (about 1e-7 relative, for

@@ -74,6 +74,10 @@ SIGNATURES = {
                                       c_void_p]),
     'lgb_dft2_plan_status': (c_int, [c_void_p, c_void_p]),
     'lgb_dft2_plan_inject_status': (c_int, [c_void_p, c_int, c_void_p]),
+    'lgb_basis_expand': (c_int, [c_void_p, c_void_p, c_int, c_size_t, c_void_p, c_void_p]),
+    'lgb_basis_project_workspace_size': (c_size_t, [c_int]),
+    'lgb_basis_project': (c_int, [c_void_p, c_void_p, c_int, c_size_t, c_void_p, c_void_p,
+                                  c_size_t, c_void_p]),
     'lgb_phasor_stack': (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int,
                                  c_int, c_double, c_int, c_void_p, c_void_p]),
     'lgb_dft2_plan_destroy': (c_int, [c_void_p]),

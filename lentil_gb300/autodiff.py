@@ -109,6 +109,33 @@ def mft_intensity(opd, amp, g):
     return MFTIntensity.apply(opd, amp, g)
 
 
+class _BasisOPD(torch.autograd.Function):
+    """OPD = sum_k c_k B_k over an FP32 basis [K, H, W], differentiable in c
+    (lgb_basis_expand / lgb_basis_project: one pass over the basis each)."""
+
+    @staticmethod
+    def forward(ctx, coeffs, basis32):
+        K, P = int(basis32.shape[0]), int(basis32[0].numel())
+        c = coeffs.detach().to(torch.float64).contiguous()
+        out = torch.empty(tuple(basis32.shape[1:]), dtype=torch.float64, device=c.device)
+        _lib.call('lgb_basis_expand', basis32.data_ptr(), c.data_ptr(), K, P, out.data_ptr(),
+                  dv.stream_ptr())
+        ctx.save_for_backward(basis32)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        (basis32,) = ctx.saved_tensors
+        K, P = int(basis32.shape[0]), int(basis32[0].numel())
+        g = grad.detach().to(torch.float64).contiguous()
+        out = torch.empty(K, dtype=torch.float64, device=g.device)
+        nb = _lib.load().lgb_basis_project_workspace_size(K)
+        ws = dv.workspace(nb)
+        _lib.call('lgb_basis_project', basis32.data_ptr(), g.data_ptr(), K, P, out.data_ptr(),
+                  ws.data_ptr(), nb, dv.stream_ptr())
+        return out, None
+
+
 class PhaseRetrieval:
     """Focus-diverse phase-retrieval loss sum_k sum (PSF_k - target_k)^2 over
     OPD = basis . coeffs (+ an optional free-form map), with the diversity
@@ -133,9 +160,15 @@ class PhaseRetrieval:
         self.device = dev
         self._graphed = None
         self._pins = None
+        # the split precisions expand the modes from an FP32 copy of the
+        # basis (half the bytes, FP32 multiply-adds); fp64 keeps torch's FP64 sum
+        self._basis32 = None if g.precision == 'fp64' else self.basis.float().contiguous()
 
     def opd(self, coeffs, free=None):
-        o = torch.einsum('k,khw->hw', coeffs, self.basis)
+        if self._basis32 is not None:
+            o = _BasisOPD.apply(coeffs, self._basis32)
+        else:
+            o = torch.einsum('k,khw->hw', coeffs, self.basis)
         return o if free is None else o + free
 
     def loss(self, coeffs, free=None):
@@ -150,7 +183,7 @@ class PhaseRetrieval:
             tgt = torch.stack(self.targets)
 
             def fn(c):
-                o = torch.einsum('k,khw->hw', c, self.basis)
+                o = self.opd(c)
                 return ((mft_intensity(o.unsqueeze(0) + div, self.amp, self.g) - tgt) ** 2).sum()
 
             sample = coeffs.detach().clone().requires_grad_(True)

@@ -1,0 +1,130 @@
+// Modal OPD expansion and its adjoint for phase retrieval (no lentil
+// counterpart: lentil has no gradients).  OPD = sum_k c_k B_k over a basis B
+// [K][P] (Zernike modes, segment piston/tip/tilt), and the coefficient
+// gradient g_k = sum_p B_k[p] dL/dOPD[p].  The basis is read as FP32 (half
+// the bytes of FP64, FP32 multiply-adds instead of this part's slow FP64
+// pipe): both passes stream the basis once and are bound by HBM.  For the
+// split-precision transforms the 1e-7 relative rounding of an FP32 product
+// is far below the 16-bit operand split that follows.
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace lgb {
+
+constexpr int BASIS_MAX_K = 1024;
+constexpr int PROJ_BLOCKS = 152;
+
+// out[p] = sum_k c[k] B[k][p]; c staged in shared memory as FP32
+__global__ void __launch_bounds__(256) basis_expand_kernel(const float* __restrict__ B,
+                                                           const double* __restrict__ c, int K,
+                                                           size_t P, double* __restrict__ out) {
+  __shared__ float cs[BASIS_MAX_K];
+  for (int k = threadIdx.x; k < K; k += blockDim.x) cs[k] = (float)c[k];
+  __syncthreads();
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P;
+       p += (size_t)gridDim.x * blockDim.x) {
+    // eight loads in flight per thread, two partial sums
+    float a0 = 0.f, a1 = 0.f;
+    int k = 0;
+    for (; k + 8 <= K; k += 8) {
+      float b[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) b[j] = __ldg(B + (size_t)(k + j) * P + p);
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        a0 = fmaf(cs[k + j], b[j], a0);
+        a1 = fmaf(cs[k + j + 1], b[j + 1], a1);
+      }
+    }
+    for (; k < K; ++k) a0 = fmaf(cs[k], __ldg(B + (size_t)k * P + p), a0);
+    out[p] = (double)(a0 + a1);
+  }
+}
+
+constexpr int PROJ_KG = 8;        // modes per block of the projection
+
+// partial[k][chunk] = sum over pixel chunk blockIdx.x of B[k][p] g[p], for
+// the PROJ_KG modes of blockIdx.y: each thread loads g[p] once for all of
+// them and keeps one sum per mode; one fixed-order block reduction at the end
+__global__ void __launch_bounds__(256) basis_project_partial_kernel(const float* __restrict__ B,
+                                                                    const double* __restrict__ g,
+                                                                    int K, size_t P,
+                                                                    double* __restrict__ partial) {
+  __shared__ double red[8][PROJ_KG];
+  const int k0 = blockIdx.y * PROJ_KG, nk = min(PROJ_KG, K - k0);
+  const size_t per = (P + gridDim.x - 1) / gridDim.x;
+  const size_t p0 = (size_t)blockIdx.x * per, p1 = min(P, p0 + per);
+  // a thread sums only a few pixels (P / gridDim.x / blockDim.x): FP32 there,
+  // FP64 from the warp reduction on (this part's FP64 adds are as slow as FMAs)
+  float acc[PROJ_KG];
+#pragma unroll
+  for (int j = 0; j < PROJ_KG; ++j) acc[j] = 0.f;
+  for (size_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+    const float gv = (float)g[p];
+#pragma unroll
+    for (int j = 0; j < PROJ_KG; ++j)
+      if (j < nk) acc[j] = fmaf(__ldg(B + (size_t)(k0 + j) * P + p), gv, acc[j]);
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < PROJ_KG; ++j) {
+    double v = (double)acc[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[w][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nk) {
+    double t = 0.0;
+    for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww) t += red[ww][threadIdx.x];
+    partial[(size_t)(k0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+__global__ void basis_project_final_kernel(const double* __restrict__ partial, int nblocks, int K,
+                                           double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  double t = 0.0;
+  for (int b = 0; b < nblocks; ++b) t += partial[(size_t)k * nblocks + b];
+  out[k] = t;
+}
+
+}  // namespace lgb
+
+using namespace lgb;
+
+extern "C" int lgb_basis_expand(const float* basis, const double* coeffs, int K, size_t P,
+                                double* out, lgb_stream stream) {
+  LGB_RANGE("lgb_basis_expand");
+  LGB_REQUIRE(basis && coeffs && out, LGB_EINVAL, "basis_expand: null pointer");
+  LGB_REQUIRE(K >= 1 && K <= BASIS_MAX_K, LGB_EINVAL, "basis_expand: K outside 1..1024");
+  if (P == 0) return LGB_OK;
+  const int blocks = (int)std::max<size_t>(1, std::min<size_t>((size_t)8 * sm_count(), (P + 255) / 256));
+  basis_expand_kernel<<<blocks, 256, 0, as_stream(stream)>>>(basis, coeffs, K, P, out);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+extern "C" size_t lgb_basis_project_workspace_size(int K) {
+  return K > 0 ? (size_t)K * PROJ_BLOCKS * sizeof(double) : 0;
+}
+
+extern "C" int lgb_basis_project(const float* basis, const double* grad, int K, size_t P,
+                                 double* out, void* workspace, size_t workspace_bytes,
+                                 lgb_stream stream) {
+  LGB_RANGE("lgb_basis_project");
+  LGB_REQUIRE(basis && grad && out && workspace, LGB_EINVAL, "basis_project: null pointer");
+  LGB_REQUIRE(K >= 1 && K <= BASIS_MAX_K, LGB_EINVAL, "basis_project: K outside 1..1024");
+  LGB_REQUIRE(workspace_bytes >= lgb_basis_project_workspace_size(K), LGB_EWORKSPACE,
+              "basis_project: workspace too small");
+  double* partial = static_cast<double*>(workspace);
+  cudaStream_t s = as_stream(stream);
+  basis_project_partial_kernel<<<dim3(PROJ_BLOCKS, cdiv(K, PROJ_KG)), 256, 0, s>>>(basis, grad, K,
+                                                                                   P, partial);
+  basis_project_final_kernel<<<cdiv(K, 128), 128, 0, s>>>(partial, PROJ_BLOCKS, K, out);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}

@@ -222,3 +222,30 @@ def test_phasor_stack_forms(cuda_device):
                   m, n, 633e-9, one.data_ptr(), s)
         assert torch.equal(out[0][k], one)
     assert (out[1] - out[0]).abs().max().item() < 1e-6 * amp.max().item()
+
+
+def test_basis_expand_and_project(cuda_device):
+    # the FP32-basis modal OPD and its adjoint against torch's FP64 sums of
+    # the same FP32 basis values (ragged sizes; deterministic repeats)
+    from lentil_gb300 import _lib
+    rng = np.random.default_rng(15)
+    for K, H, W in ((1, 7, 5), (13, 33, 31), (90, 128, 96)):
+        B = torch.as_tensor(rng.normal(size=(K, H, W)), device='cuda').float()
+        c = torch.as_tensor(rng.normal(size=K), device='cuda')
+        out = torch.empty((H, W), dtype=torch.float64, device='cuda')
+        s = torch.cuda.current_stream().cuda_stream
+        _lib.call('lgb_basis_expand', B.data_ptr(), c.data_ptr(), K, H * W, out.data_ptr(), s)
+        ref = torch.einsum('k,khw->hw', c, B.double())
+        assert (out - ref).abs().max().item() < 1e-5 * ref.abs().max().item()
+        g = torch.as_tensor(rng.normal(size=(H, W)), device='cuda')
+        nb = _lib.load().lgb_basis_project_workspace_size(K)
+        ws = torch.empty(nb, dtype=torch.uint8, device='cuda')
+        res = []
+        for _ in range(2):
+            pr = torch.empty(K, dtype=torch.float64, device='cuda')
+            _lib.call('lgb_basis_project', B.data_ptr(), g.data_ptr(), K, H * W, pr.data_ptr(),
+                      ws.data_ptr(), nb, s)
+            res.append(pr)
+        assert torch.equal(res[0], res[1])
+        refp = torch.einsum('khw,hw->k', B.double(), g)
+        assert (res[0] - refp).abs().max().item() < 1e-5 * refp.abs().max().item() + 1e-12
