@@ -271,10 +271,6 @@ int launch_maxabs_amp(const double* amp, int batch, int H, int W, int r0, int c0
   return LGB_OK;
 }
 
-int launch_maxabs_c128(const double2* f, int count, float* out, cudaStream_t s) {
-  return launch_maxabs_c128_batch(f, count, 1, out, s);
-}
-
 int launch_maxabs_c128_batch(const double2* f, int count, int batch, float* out, cudaStream_t s) {
   LGB_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * batch, s));
   const int blocks = std::max(1, std::min(2 * sm_count(), cdiv(count, 256)));

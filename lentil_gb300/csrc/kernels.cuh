@@ -45,7 +45,6 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s);
 // max over the slice of |amp| (phasor mode) or max(|re|,|im|) (complex mode)
 int launch_maxabs_amp(const double* amp, int batch, int H, int W, int r0, int c0, int m, int n,
                       float* out, cudaStream_t s);
-int launch_maxabs_c128(const double2* f, int count, float* out, cudaStream_t s);
 // per field b < batch of `count` entries each: out[b] = max(|re|, |im|)
 int launch_maxabs_c128_batch(const double2* f, int count, int batch, float* out, cudaStream_t s);
 

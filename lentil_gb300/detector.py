@@ -1,6 +1,5 @@
 """Detector sampling on the GPU, drop-in for ``lentil.detector.pixel`` and
 ``lentil.detector.pixelate`` (lentil/detector.py:167-251)."""
-import numpy as np
 import torch
 
 from . import _device as dv
