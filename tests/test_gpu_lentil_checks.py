@@ -1,0 +1,104 @@
+"""The physical checks lentil's own propagation tests make (lentil
+tests/test_propagate.py:8-141), restated here and run through the GPU path:
+power conservation, the Airy pattern of a circular pupil, the centroid's
+invariance under fit_tilt, the analytic image shift of a pupil tilt, and an
+all-zero image when the tilt moves the PSF out of the window.  Seeded, and
+in both the complex128 and the split tensor-core forms where the check is
+not an exact equality."""
+import numpy as np
+import pytest
+import scipy.special
+
+import lentil_gb300 as lg
+from oracle import lentil_oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+PRECISIONS = ['fp64', 'split-bf16']
+
+
+def _pupil(npix, radius, coeffs=None, focal_length=10.0, diameter=1.0):
+    """Circular pupil of unit power with a Zernike OPD, `diameter` across
+    2 * radius pixels."""
+    amp = lo.normalize_power(lg.circle((npix, npix), radius))
+    opd = np.zeros((npix, npix)) if coeffs is None else lg.zernike_compose(amp > 0, coeffs)
+    return lg.Pupil(amplitude=amp, opd=opd, pixelscale=diameter / (2 * radius),
+                    focal_length=focal_length)
+
+
+def _psf(p, lam, shape, pixelscale, oversample, precision):
+    w = lg.propagate_dft(lg.Wavefront(lam) * p, pixelscale=pixelscale, shape=shape,
+                         oversample=oversample, precision=precision)
+    return w.intensity
+
+
+def _airy(diameter, focal_length, lam, pixelscale, n):
+    """(2 J1(x) / x)^2 with x = pi q D / (lam f), centred on pixel (n-1)/2."""
+    c = (n - 1) / 2.0
+    y, x = np.indices((n, n), dtype=float)
+    q = np.hypot((x - c) * pixelscale, (y - c) * pixelscale)
+    arg = np.pi * q * diameter / (lam * focal_length)
+    arg[arg == 0] = np.finfo(float).eps
+    return (2 * scipy.special.j1(arg) / arg) ** 2
+
+
+@pytest.mark.parametrize('precision', PRECISIONS)
+@pytest.mark.parametrize('oversample', [1, 2])
+def test_power_is_conserved(cuda_device, precision, oversample):
+    psf = _psf(_pupil(256, 120), 650e-9, (64, 64), 5e-6, oversample, precision)
+    assert 0.95 <= psf.sum() <= 1.0 + 1e-9
+
+
+@pytest.mark.parametrize('precision', PRECISIONS)
+def test_airy_pattern(cuda_device, precision):
+    p = _pupil(512, 250)
+    psf = _psf(p, 650e-9, 511, 5e-6, 1, precision)          # odd: the DC pixel is central
+    ref = _airy(1.0, 10.0, 650e-9, 5e-6, 511)
+    assert np.allclose(psf / psf.max(), ref / ref.max(), atol=1e-3)
+
+
+def _tilt_coeffs(seed):
+    c = 5e-6 * np.random.default_rng(seed).uniform(-0.5, 0.5, 3)
+    c[0] = 0.0
+    return c
+
+
+@pytest.mark.parametrize('seed', [1, 2, 3])
+def test_fit_tilt_keeps_the_centroid(cuda_device, seed):
+    coeffs = _tilt_coeffs(seed)
+    p = _pupil(256, 120, coeffs)
+    psf = _psf(p, 650e-9, 128, 5e-6, 2, 'fp64')
+    p.fit_tilt(inplace=True)
+    psf_fit = _psf(p, 650e-9, 128, 5e-6, 2, 'fp64')
+    psf[psf < 1e-5] = 0
+    psf_fit[psf_fit < 1e-5] = 0
+    delta = np.abs(np.asarray(lo.centroid(psf)) - np.asarray(lo.centroid(psf_fit)))
+    assert np.all(delta <= 1e-10)
+
+
+@pytest.mark.parametrize('fit', [False, True])
+@pytest.mark.parametrize('seed', [4, 5])
+def test_tilt_shift_matches_geometry(cuda_device, fit, seed):
+    # a Noll Z2/Z3 coefficient c tilts the wavefront by 4c peak-to-valley
+    # across the diameter: the image moves by (4c / D) f / pixel, (x, y) ->
+    # (row, col) = (y, -x)
+    os_, ps, npix = 10, 5e-6, 64
+    coeffs = _tilt_coeffs(seed)
+    p = _pupil(256, 120, coeffs)
+    if fit:
+        p.fit_tilt(inplace=True)
+    psf = _psf(p, 650e-9, (npix, npix), ps, os_, 'fp64')
+    psf = psf / psf.max()
+    psf[psf < 0.2] = 0
+    shift = np.asarray(lo.centroid(psf)) - npix // 2 * os_
+    tilt = coeffs[1:3]
+    expect = (tilt / 1.0) * 10.0 / ps * os_ * 4
+    expect = np.array([expect[1], -expect[0]])
+    assert np.all(np.abs(shift - expect) / os_ < 0.2)
+
+
+def test_tilt_out_of_the_window_gives_no_image(cuda_device):
+    p = _pupil(255, 120, [0, 1e-3])
+    p.fit_tilt(inplace=True)
+    img = _psf(p, 650e-9, (64, 64), 5e-6, 2, 'fp64')
+    assert np.all(img == 0)
