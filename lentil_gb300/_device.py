@@ -6,10 +6,18 @@ import torch
 from . import _lib
 
 
+_ready = False
+
+
 def device():
-    if not torch.cuda.is_available():
-        raise RuntimeError('lentil_gb300 needs a CUDA device (GB300, sm_103a); none is available')
-    _lib.load()
+    """The current CUDA device; raises when there is none (no CPU fallback).
+    The availability check and the library load run once per process."""
+    global _ready
+    if not _ready:
+        if not torch.cuda.is_available():
+            raise RuntimeError('lentil_gb300 needs a CUDA device (GB300, sm_103a); none is available')
+        _lib.load()
+        _ready = True
     return torch.device('cuda', torch.cuda.current_device())
 
 

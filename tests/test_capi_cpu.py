@@ -108,3 +108,19 @@ def test_dft2_plan_argument_errors_without_a_gpu(lib):
 
 def test_build_is_up_to_date():
     assert _build.up_to_date()
+
+
+def test_no_cpu_fallback():
+    # without a CUDA device every entry of the path raises instead of
+    # computing on the host (this container has no GPU)
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip('a CUDA device is present')
+    import lentil_gb300 as lg
+    f = np.ones((8, 8), dtype=complex)
+    for call in (lambda: lg.fourier.dft2(f, 0.1),
+                 lambda: lg.fourier.dft2_batch(f[None], 0.1, precision='split-bf16'),
+                 lambda: lg.detector.pixelate(np.ones((8, 8)), 2),
+                 lambda: lg.zernike_compose(np.ones((8, 8)), [0, 1e-8])):
+        with pytest.raises(RuntimeError, match='CUDA device'):
+            call()
