@@ -318,16 +318,13 @@ def idft2(F, alpha, shape=None, shift=(0, 0), unitary=True, out=None, npix=None,
     Fd = dv.to_device(F, torch.complex128)
     if Fd.dim() != 2:
         raise ValueError('idft2 expects a 2-D array')
-    m, n = Fd.shape
+    m, n = (int(x) for x in Fd.shape)
     M, N = _shape(shape, npix, (m, n))
-    ar, ac = _pair(alpha, 'alpha')
-    sr, sc = _pair(shift, 'shift')
-    prec = _lib.precision_code(precision)
-    f = torch.empty((M, N), dtype=torch.complex128, device=Fd.device)
-    nbytes = _lib.load().lgb_idft2_workspace_size(m, n, M, N, prec)
-    ws = dv.workspace(nbytes)
-    _lib.call('lgb_idft2', Fd.data_ptr(), m, n, f.data_ptr(), M, N, ar, ac, sr, sc,
-              int(bool(unitary)), prec, ws.data_ptr(), nbytes, dv.stream_ptr())
-    if prec != _lib.FP64:
-        _lib.call('lgb_dft2_status', ws.data_ptr(), dv.stream_ptr())
-    return _finish(f, out, host)
+    # conj(dft2(conj(F), offset 0)) * (1 / F.size), the dft2 from the plan cache
+    G, plan = _transform(Fd.conj().resolve_conj().unsqueeze(0), M, N, alpha, shift, (0, 0),
+                         unitary, precision)
+    f = G[0].conj() * (1.0 / (m * n))
+    res = _finish(f, out, host)
+    if plan.split and (host or (out is not None and not dv.is_tensor(out))):
+        plan.status()
+    return res

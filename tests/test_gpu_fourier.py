@@ -245,3 +245,23 @@ def test_plan_status_is_reported_by_the_next_execute(cuda_device):
     with pytest.raises(ValueError):
         _lib.call('lgb_dft2_plan_inject_status', plan._h, 3, lg._device.stream_ptr())
     fourier.clear_plan_cache()
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'split-fp16'])
+def test_idft2_repeated_uses_the_plan_cache(cuda_device, precision):
+    # idft2 = conj(dft2(conj(F))) / F.size through the same plan cache: the
+    # second call of a geometry runs from a plan and gives the same result
+    fourier = lg.fourier
+    fourier.clear_plan_cache()
+    rng = np.random.default_rng(16)
+    F = rng.standard_normal((30, 44)) + 1j * rng.standard_normal((30, 44))
+    kw = dict(shape=(36, 25), shift=(0.5, -1.0), unitary=True)
+    a = fourier.idft2(F, (0.03, 0.02), precision=precision, **kw)
+    b = fourier.idft2(F, (0.03, 0.02), precision=precision, **kw)
+    assert fourier.plan_cache_info()[0] == 1
+    same = 1e-15 if precision == 'fp64' else 1e-12
+    assert lo.peak_normalised_error(b, a) < same
+    ref = lo.idft2(F, (0.03, 0.02), **kw)
+    tol = FP64_TOL if precision == 'fp64' else SPLIT_TOL[precision]
+    assert lo.peak_normalised_error(b, ref) < tol
+    fourier.clear_plan_cache()
