@@ -178,3 +178,21 @@ def test_zernike_tilt_and_power_spectrum(cuda_device):
                   3.0, psd.ptr, pws.ptr, pb, _s())
         psd.check()
         pws.check()
+
+
+@pytest.mark.parametrize('precision', [_lib.FP64, _lib.SPLIT_BF16])
+def test_idft2_c_entry(cuda_device, precision):
+    # lgb_idft2 (the C entry; Python's idft2 composes the cached dft2 instead)
+    lib = _lib.load()
+    m, n, M, N = 33, 47, 40, 29
+    F = _c128((m, n), 5)
+    out = Guarded(16 * M * N)
+    nbytes = lib.lgb_idft2_workspace_size(m, n, M, N, precision)
+    ws = Guarded(nbytes)
+    _lib.call('lgb_idft2', F.data_ptr(), m, n, out.ptr, M, N, 0.03, 0.025, 0.5, -1.0, 1,
+              precision, ws.ptr, nbytes, _s())
+    out.check()
+    ws.check()
+    got = out.view(torch.complex128, (M, N)).cpu().numpy()
+    ref = lo.idft2(F.cpu().numpy(), (0.03, 0.025), shape=(M, N), shift=(0.5, -1.0), unitary=True)
+    assert lo.peak_normalised_error(got, ref) < (1e-12 if precision == _lib.FP64 else 3e-5)
