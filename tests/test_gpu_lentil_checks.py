@@ -102,3 +102,42 @@ def test_tilt_out_of_the_window_gives_no_image(cuda_device):
     p.fit_tilt(inplace=True)
     img = _psf(p, 650e-9, (64, 64), 5e-6, 2, 'fp64')
     assert np.all(img == 0)
+
+
+@pytest.mark.parametrize('precision', PRECISIONS)
+@pytest.mark.parametrize('coeffs,size', [(None, 128), ([0, 1e-6, 2e-6], 64)])
+def test_mask_equals_masked_psf(cuda_device, precision, coeffs, size):
+    # lentil tests/test_propagate_mask.py:4-37: propagating into a detector
+    # mask gives the unmasked PSF times the mask (with and without tilt)
+    p = _pupil(256, 120, coeffs)
+    mask = lg.rectangle((256, 256), size, size, shift=(20, -30), antialias=False)
+    psf = _psf(p, 650e-9, 128, 5e-6, 2, precision)
+    w = lg.propagate_dft(lg.Wavefront(650e-9) * p, pixelscale=5e-6, shape=128, oversample=2,
+                         mask=mask, precision=precision)
+    if precision == 'fp64':
+        assert np.allclose(w.intensity, psf * mask)
+    else:
+        # two different transform sizes, each within 2e-6 of the exact PSF
+        assert lo.peak_normalised_error(w.intensity, psf * mask) < 4e-6
+
+
+@pytest.mark.parametrize('precision', PRECISIONS)
+@pytest.mark.parametrize('seed', [0, 3])
+def test_rescaled_pupil_gives_the_same_psf(cuda_device, precision, seed):
+    # lentil tests/test_propagate.py:144-163: a pupil resampled 3x finer
+    # (lentil Plane.rescale: cubic spline, amplitude / scale, pixelscale /
+    # scale; prepared here with the oracle's rescale) gives a PSF whose
+    # cross-correlation with the original peaks at zero lag and whose power
+    # agrees to 1%
+    coeffs = np.random.default_rng(seed).uniform(-200e-9, 200e-9, 6)
+    amp = lo.normalize_power(lg.circle((256, 256), 120))
+    opd = lo.zernike_compose(amp > 0, coeffs)
+    amp2 = lo.rescale(amp, 3, order=3, mode='nearest', unitary=False) / 3
+    opd2 = lo.rescale(opd, 3, order=3, mode='nearest', unitary=False)
+    psfs = []
+    for a, o, ps in ((amp, opd, 1.0 / 240), (amp2, opd2, 1.0 / 720)):
+        p = lg.Pupil(amplitude=a, opd=o, pixelscale=ps, focal_length=10.0)
+        psfs.append(_psf(p, 650e-9, (64, 64), 5e-6, 10, precision))
+    xc = np.fft.ifftshift(np.conj(np.fft.fft2(psfs[0])) * np.fft.fft2(psfs[1]))
+    assert np.allclose(lo.centroid(np.abs(xc)), [320, 320])
+    assert np.isclose(psfs[0].sum(), psfs[1].sum(), rtol=1e-2)
