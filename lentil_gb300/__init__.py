@@ -17,7 +17,7 @@ from . import fourier
 from . import detector
 from . import field
 from .field import Field
-from .plane import Plane, Pupil, Image, Tilt
+from .plane import Plane, Pupil, Image, Tilt, DispersiveTilt, Grism
 from .wavefront import Wavefront
 from .propagate import propagate_dft, propagate_fft, scratch_shape
 from .broadband import broadband_psf, PSFPlan

@@ -414,3 +414,91 @@ class Tilt(_TiltBase):
 
     def __shift__(self, xs=0, ys=0, z=0, **kwargs):
         return xs - z * self.x, ys - z * self.y
+
+
+_GL_NODES, _GL_WEIGHTS = np.polynomial.legendre.leggauss(32)
+
+
+class DispersiveTilt(_TiltBase):
+    """Spectral dispersion as a wavelength-dependent image shift
+    (lentil/plane.py:926-1097).
+
+    The light of wavelength ``lam`` lands at distance ``d`` along the
+    spectral trace, with ``lam = polyval(dispersion, d)``, at the trace
+    point ``(x, polyval(trace, x))`` whose arc length from ``x = 0`` is
+    ``d``; the shift adds that point to the incoming one.  Both polynomials
+    are in decreasing powers, lengths in meters on the focal plane.
+
+    First-order polynomials are solved in closed form, with lentil's
+    arithmetic.  For higher orders ``d`` is the real root of
+    ``polyval(dispersion, d) - lam`` nearest zero (companion-matrix roots
+    polished by Newton steps) and ``x`` inverts the arc length
+    ``s(x) = integral_0^x sqrt(1 + trace'(t)^2) dt`` by Newton's method over
+    32-point Gauss-Legendre quadrature.  (lentil reaches the same points by
+    least squares from 0; under numpy 2 its higher-order trace raises a
+    TypeError there.)"""
+
+    def __init__(self, trace=None, dispersion=None, **kwargs):
+        super().__init__(**kwargs)
+        if trace is not None:
+            self.trace = np.asarray(trace)
+        if dispersion is not None:
+            self.dispersion = np.asarray(dispersion)
+
+    def __shift__(self, wavelength, xs=0., ys=0., **kwargs):
+        trace = np.asarray(self.trace, dtype=float)
+        x = self._trace_x(trace, self._distance(np.asarray(self.dispersion, dtype=float),
+                                                float(wavelength)))
+        return x + xs, np.polyval(trace, x) + ys
+
+    @staticmethod
+    def _distance(disp, lam):
+        if disp.size == 2:
+            return (lam - disp[1]) / disp[0]
+        if disp.size < 2:
+            raise ValueError('dispersion needs order >= 1')
+        c = disp.copy()
+        c[-1] -= lam
+        r = np.roots(c)
+        r = r[np.abs(r.imag) <= 1e-9 * np.maximum(np.abs(r), 1e-300)].real
+        if r.size == 0:
+            raise ValueError(f'no distance along the trace has wavelength {lam}')
+        d = r[np.argmin(np.abs(r))]
+        dc = np.polyder(c)
+        for _ in range(3):
+            g = np.polyval(dc, d)
+            if g == 0:
+                break
+            d = d - np.polyval(c, d) / g
+        return float(d)
+
+    @staticmethod
+    def _trace_x(trace, d):
+        if trace.size == 2:
+            return d / np.sqrt(1 + trace[0] ** 2)
+        slope = np.polyder(trace) if trace.size > 1 else np.zeros(1)
+
+        def speed(t):
+            return np.sqrt(1.0 + np.polyval(slope, t) ** 2)
+
+        def arc(x):
+            h = 0.5 * x
+            return h * np.dot(_GL_WEIGHTS, speed(h * (_GL_NODES + 1.0)))
+
+        x = d / speed(0.0)
+        for _ in range(60):
+            step = (arc(x) - d) / speed(x)
+            x -= step
+            if abs(step) <= 4e-16 * max(abs(x), 1e-300):
+                break
+        return float(x)
+
+
+class Grism(DispersiveTilt):
+    """Deprecated alias of :class:`DispersiveTilt` (lentil/plane.py:1099-1169)."""
+
+    def __init__(self, trace, dispersion, **kwargs):
+        import warnings
+        warnings.warn('lentil.Grism will be deprecated in v1.0.0, it is replaced by '
+                      'lentil.DispersiveTilt.', DeprecationWarning, stacklevel=2)
+        super().__init__(trace=trace, dispersion=dispersion, **kwargs)

@@ -291,6 +291,55 @@ def main(ref_root):
     q['scratch_shape'] = np.asarray(lentil.scratch_shape([500e-9, 650e-9, 900e-9], 1 / 256,
                                                          5e-6, 10, 2))
     np.savez_compressed(os.path.join(HERE, 'propagate_fft.npz'), **q)
+
+    # ------------------------------------------- tilt planes (grism, Tilt)
+    # own generator so that the fixtures above do not change
+    rt = np.random.default_rng(20261205)
+    t = {}
+    # name: (trace, dispersion); meters on the focal plane, meters of
+    # wavelength.  lentil 0.8.8 cannot evaluate a trace of order > 1 under
+    # numpy 2 (leastsq hands scipy's quad a 1-element array: TypeError), so
+    # the fixtures hold first-order traces only; a dispersion of order > 1
+    # evaluates (__shift__ below) but its 1-element shift then fails in
+    # propagate_dft's window arithmetic, so the images use first-order grisms
+    grisms = {
+        'lin': ([0.3, 0.0], [1e-3, 650e-9]),
+        'steep': ([-2.5, 0.0], [8e-4, 600e-9]),
+        'quad_disp': ([0.3, 0.0], [2.0, 1e-3, 650e-9]),
+        'cubic_disp': ([0.0, 0.0], [-50.0, 1.5, 1.2e-3, 640e-9]),
+    }
+    wl = np.linspace(550e-9, 750e-9, 9)
+    starts = np.array([[0.0, 0.0], [1e-6, -2e-6]])
+    for name, (trace, disp) in grisms.items():
+        dt = lentil.DispersiveTilt(trace=trace, dispersion=disp)
+        xy = np.empty((len(starts), len(wl), 2))
+        for i, (xs, ys) in enumerate(starts):
+            for j, lam in enumerate(wl):
+                x, y = dt.__shift__(wavelength=lam, xs=xs, ys=ys)
+                xy[i, j] = float(np.squeeze(x)), float(np.squeeze(y))
+        t[f'{name}_trace'] = np.asarray(trace, float)
+        t[f'{name}_dispersion'] = np.asarray(disp, float)
+        t[f'{name}_xy'] = xy
+    t['wl'], t['starts'] = wl, starts
+    # dispersed broadband images through lentil's loop, and a plain Tilt plane
+    amp = lentil.normalize_power(lentil.circle((64, 64), 30))
+    opd = lentil.zernike_compose(amp, np.concatenate([[0.0], rt.normal(0, 30e-9, 6)]))
+    pl = lentil.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 60, focal_length=10)
+    t['img_amp'], t['img_opd'] = amp, opd
+    t['img_wl'] = np.linspace(600e-9, 700e-9, 5)
+    t['img_wt'] = rt.uniform(0.5, 1.0, 5)
+    planes = {'lin': lentil.DispersiveTilt(trace=grisms['lin'][0], dispersion=grisms['lin'][1]),
+              'steep': lentil.DispersiveTilt(trace=grisms['steep'][0],
+                                             dispersion=grisms['steep'][1]),
+              'tilt': lentil.Tilt(x=2.3e-6, y=-1.1e-6)}
+    for name, tp in planes.items():
+        img = np.zeros((96, 96))
+        for lam, w8 in zip(t['img_wl'], t['img_wt']):
+            w = lentil.propagate_dft(lentil.Wavefront(lam) * pl * tp, pixelscale=6e-6, shape=48,
+                                     oversample=2)
+            img = w.insert(img, weight=w8)
+        t[f'img_{name}'] = img
+    np.savez_compressed(os.path.join(HERE, 'tilt.npz'), **t)
     print('golden fixtures written to', HERE)
 
 

@@ -272,3 +272,22 @@ def test_image_to_pupil_round_trip(cuda_device):
     got, ref = out['lentil_gb300'], out[lo.__name__]
     assert got.shape == ref.shape == (96, 96)
     assert lo.peak_normalised_error(got, ref) < 1e-12
+
+
+@pytest.mark.parametrize('name', ['lin', 'steep', 'tilt'])
+@pytest.mark.parametrize('precision,tol', [('fp64', 1e-12), ('split-bf16', 2e-6)])
+def test_tilt_planes_golden(golden, cuda_device, name, precision, tol):
+    # Wavefront * pupil * (DispersiveTilt | Tilt) through lentil's broadband
+    # loop: each wavelength lands at its own window (a dispersed spectrum)
+    g = golden('tilt')
+    pl = lg.Pupil(amplitude=g['img_amp'], opd=g['img_opd'], pixelscale=1 / 60, focal_length=10)
+    if name == 'tilt':
+        tp = lg.Tilt(x=2.3e-6, y=-1.1e-6)
+    else:
+        tp = lg.DispersiveTilt(trace=g[f'{name}_trace'], dispersion=g[f'{name}_dispersion'])
+    img = np.zeros((96, 96))
+    for lam, wt in zip(g['img_wl'], g['img_wt']):
+        w = lg.propagate_dft(lg.Wavefront(lam) * pl * tp, pixelscale=6e-6, shape=48, oversample=2,
+                             precision=precision)
+        img = w.insert(img, weight=wt)
+    assert lo.peak_normalised_error(img, g[f'img_{name}']) < tol
