@@ -141,3 +141,24 @@ def test_rescaled_pupil_gives_the_same_psf(cuda_device, precision, seed):
     xc = np.fft.ifftshift(np.conj(np.fft.fft2(psfs[0])) * np.fft.fft2(psfs[1]))
     assert np.allclose(lo.centroid(np.abs(xc)), [320, 320])
     assert np.isclose(psfs[0].sum(), psfs[1].sum(), rtol=1e-2)
+
+
+def test_error_behaviour(cuda_device):
+    # the exception types lentil raises on the path: ptype misuse
+    # (lentil/plane.py:478-481, wavefront.py:96-97, propagate.py:266-267),
+    # mask shape (propagate.py:184-185), out dtype (fourier.py:91-93), FFT
+    # propagation with tilt (propagate.py:36-38)
+    with pytest.raises(TypeError):
+        lg.Wavefront(650e-9, ptype=lg.image) * lg.Pupil()
+    with pytest.raises(TypeError):
+        lg.Wavefront(650e-9, ptype=lg.tilt)
+    with pytest.raises(TypeError):
+        lg.propagate_dft(lg.Wavefront(650e-9), 5e-6, shape=32)
+    p = _pupil(64, 30)
+    with pytest.raises(ValueError):
+        lg.propagate_dft(lg.Wavefront(650e-9) * p, 5e-6, shape=32, oversample=2,
+                         mask=np.ones((10, 10)))
+    with pytest.raises(TypeError):
+        lg.fourier.dft2(np.ones((4, 4)), 0.1, out=np.zeros((4, 4)))
+    with pytest.raises(NotImplementedError):
+        lg.propagate_fft(lg.Wavefront(650e-9) * p * lg.Tilt(1e-6, 0), 5e-6, shape=32)
