@@ -99,18 +99,22 @@ int launch_phasor_batch_c128(const double* amp, const double* opd, int H, int W,
 // Output row c (field column), K index r (field row) for the real part and
 // kp + r for the imaginary part: f^T in the stage-1 B-operand layout.
 // One block = 64 field rows x 32 field columns and a contiguous group of
-// wavelengths (blockIdx.z = PSF * groups + group): splitting the wavelength
-// loop over blocks keeps enough blocks in flight to cover HBM latency.  The
-// transpose tile is double-buffered, so each wavelength needs one barrier.
+// wavelengths (blockIdx.x = row tile * groups + group, blockIdx.z = PSF).
+// Splitting the wavelength loop over blocks keeps enough blocks in flight to
+// cover HBM latency; the groups of one tile are adjacent in launch order, so
+// that their re-reads of amp and opd hit L2.  The transpose tile is
+// double-buffered, so each wavelength needs one barrier.
 // ---------------------------------------------------------------------------
 constexpr int TR = 64, TC = 32, TPAD = 8;
 
 template <bool BF16, bool PHASOR>
 __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, int groups) {
   __shared__ __align__(16) uint16_t tile[2][4][TC][TR + TPAD];   // re_hi, re_lo, im_hi, im_lo
+  __shared__ int warp_nz[8];
   const int tid = threadIdx.x;
-  const int rt = blockIdx.x * TR, ct = blockIdx.y * TC;
-  const int b = blockIdx.z / groups, g = blockIdx.z - b * groups;   // PSF, wavelength group
+  const int rtile = blockIdx.x / groups, g = blockIdx.x - rtile * groups;   // row tile, group
+  const int rt = rtile * TR, ct = blockIdx.y * TC;
+  const int b = blockIdx.z;                                                 // PSF
   const float sf = pow2_scale_for(a.maxabs[b]);
 
   // thread (w, lane) owns field column ct + lane and rows rt + 8w .. 8w+7:
@@ -134,6 +138,27 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
         const double2 v = a.field[((size_t)b * a.m + r) * a.n + c];
         fv[k] = make_float2((float)v.x * sf, (float)v.y * sf);
       }
+    }
+  }
+
+  // nonzero flags of the block's two 32-row halves x 32 columns (warps 0-3
+  // hold rows 0-31, warps 4-7 rows 32-63); the first wavelength group
+  // writes them, and the last column block also zeroes the padding columns
+  if (a.kflags) {
+    bool nz = false;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      nz |= PHASOR ? amp_r[k] != 0.f : (fv[k].x != 0.f || fv[k].y != 0.f);
+    nz = __any_sync(0xffffffffu, nz);
+    if (lane == 0) warp_nz[w] = nz;
+    __syncthreads();
+    const int units = a.kp / 32, u = 2 * rtile + tid;
+    if (g == 0 && tid < 2 && u < units) {
+      uint8_t* row = a.kflags + ((size_t)b * units + u) * a.kf_pitch;
+      row[blockIdx.y] = (warp_nz[4 * tid] | warp_nz[4 * tid + 1] | warp_nz[4 * tid + 2] |
+                         warp_nz[4 * tid + 3]) != 0;
+      if (blockIdx.y == gridDim.y - 1)
+        for (int c = gridDim.y; c < a.kf_pitch; ++c) row[c] = 0;
     }
   }
 
@@ -192,13 +217,17 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
 }
 
 int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
+  LGB_REQUIRE(!a.kflags || (a.kp % 32 == 0 && a.kf_pitch % 8 == 0 && a.kf_pitch >= cdiv(a.n, TC)),
+              LGB_EINVAL, "split field: flag rows must hold every 32-column piece");
   const int spatial = cdiv(a.kp, TR) * cdiv(a.n, TC);
   const int psfs = a.batch;
   const int L = a.amp ? a.L : 1;
   // Wavelength groups: each group re-reads the block's amp/opd once, and
   // the blocks run in waves of `cap` resident blocks; pick the group count
-  // that minimises whole waves per wavelength of work (the last wave of a
-  // launch is otherwise partly empty), among counts up to 16.
+  // that minimises whole waves times the work of one block (the last wave
+  // of a launch is otherwise partly empty), among counts up to 16.  A
+  // block's fixed part (loading amp and opd, the flags) counts as two
+  // wavelengths of work.
   int per_sm = 0;
   auto kfn = bf16 ? (a.amp ? split_field_T_kernel<true, true> : split_field_T_kernel<true, false>)
                   : (a.amp ? split_field_T_kernel<false, true> : split_field_T_kernel<false, false>);
@@ -210,12 +239,12 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
   double best = 1e300;
   for (int g = 1; g <= std::min(L, 16); ++g) {
     const long long waves = (base * g + cap - 1) / cap;
-    const double cost = (double)waves * (double)cdiv(L, g);    // waves x wavelengths per block
+    const double cost = (double)waves * (double)(cdiv(L, g) + 2);   // waves x work per block
     if (cost < best * (1.0 - 1e-9)) { best = cost; groups = g; }
   }
   groups = cdiv(L, cdiv(L, groups));                 // no empty trailing group
-  LGB_REQUIRE((long long)psfs * groups <= 65535, LGB_EINVAL, "split field: too many PSFs in one launch");
-  dim3 grid(cdiv(a.kp, TR), cdiv(a.n, TC), psfs * groups);
+  LGB_REQUIRE(psfs <= 65535, LGB_EINVAL, "split field: too many PSFs in one launch");
+  dim3 grid(cdiv(a.kp, TR) * groups, cdiv(a.n, TC), psfs);
   if (a.amp) {
     if (bf16) split_field_T_kernel<true, true><<<grid, 256, 0, s>>>(a, groups);
     else split_field_T_kernel<false, true><<<grid, 256, 0, s>>>(a, groups);

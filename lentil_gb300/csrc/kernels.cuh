@@ -39,6 +39,10 @@ struct SplitFieldArgs {
   uint16_t* hi;            // [batch*L][n][2*kp]
   uint16_t* lo;
   const int* lam_idx;      // optional [L] device: wavelength -> khalf slot
+  // optional: nonzero flags of the field's 32 x 32 pieces, [batch][kp/32][kf_pitch]
+  // bytes (written in full, padding columns included), for the MFT's K-block skip
+  uint8_t* kflags;
+  int kf_pitch;            // multiple of 8, >= 8 * ceil(kp2 / 256)
 };
 int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s);
 
@@ -91,7 +95,14 @@ struct SplitMftProblem {
   const int* lam_idx;      // optional [L] device: wavelength -> DFT-matrix slot
   int L_bank;              // DFT-matrix slots held (when lam_idx is set)
   int tile;                // pair-tile width 256 or 128; 0: the autotuner's choice
+  // optional stage-1 K-block skip: the field's nonzero flags as written by
+  // the split operand kernel ([batch][kp1/32][kf_pitch]); null: dense
+  const uint8_t* kflags;
+  int kf_pitch;
 };
+// bytes of a field-flag row (32-column pieces of a kp2-wide operand, padded
+// to whole 256-column tiles)
+inline int kflag_pitch(int kp2) { return 8 * ((kp2 + 255) / 256); }
 int launch_split_mft(const SplitMftProblem& p, cudaStream_t s);
 // scale applied to the stage-1 result before its 16-bit split
 float split_g_scale(int m);

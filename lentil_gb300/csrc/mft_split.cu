@@ -123,6 +123,9 @@ struct Params {
   double cscale;
   int* err;
   const int* lam_idx;        // [L] wavelength -> DFT-matrix slot, or null (identity)
+  const uint8_t* kflags;     // stage 1: field nonzero flags [batch][kf_units][kf_pitch], or null
+  int kf_units;              // kp1 / 32 (== kblocks)
+  int kf_pitch;
 };
 
 // MMA N of column tile tn: BN, except a narrower last tile when the
@@ -325,6 +328,55 @@ __device__ __forceinline__ Item decode(const Params& p, int i) {
   return it;
 }
 
+// ------------------------------------------------------ K-block skipping ---
+// Stage 1 with field flags: a K block whose field rows are zero across the
+// item's whole column tile adds nothing and is skipped, by the producer, the
+// MMA issuer and the epilogues alike (each derives the same set from the
+// same flags).  K block kb covers the 32-row K units 2kb and 2kb + 1; K unit
+// u is field unit u mod kf_units (the real rows, then the imaginary rows).
+// Up to 128 K blocks are tracked; beyond that the host passes no flags.
+struct Live {
+  uint64_t lo, hi;           // bit kb: K block kb is issued
+  int n;                     // K blocks issued
+  bool all;
+};
+
+template <int BN>
+__device__ __forceinline__ Live live_kblocks(const Params& p, const Item& w) {
+  Live lv{~0ull, ~0ull, p.kblocks, true};
+  if (!p.kflags) return lv;
+  uint64_t ulo = 0, uhi = 0;                 // bit u: field unit u is nonzero in the tile
+  const uint8_t* f = p.kflags + (size_t)w.psf * p.kf_units * p.kf_pitch + w.tn * (BN / 32);
+#pragma unroll 8
+  for (int u = 0; u < p.kf_units; ++u) {
+    const uint8_t* fu = f + (size_t)u * p.kf_pitch;
+    const bool nz = BN == 256 ? __ldg(reinterpret_cast<const unsigned long long*>(fu)) != 0ull
+                              : __ldg(reinterpret_cast<const unsigned int*>(fu)) != 0u;
+    if (nz) {
+      if (u < 64) ulo |= 1ull << u;
+      else uhi |= 1ull << (u - 64);
+    }
+  }
+  lv = Live{0ull, 0ull, 0, false};
+  for (int kb = 0; kb < p.kblocks; ++kb) {
+    int u0 = 2 * kb, u1 = 2 * kb + 1;
+    if (u0 >= p.kf_units) u0 -= p.kf_units;
+    if (u1 >= p.kf_units) u1 -= p.kf_units;
+    const uint64_t b0 = u0 < 64 ? ulo >> u0 : uhi >> (u0 - 64);
+    const uint64_t b1 = u1 < 64 ? ulo >> u1 : uhi >> (u1 - 64);
+    if ((b0 | b1) & 1ull) {
+      if (kb < 64) lv.lo |= 1ull << kb;
+      else lv.hi |= 1ull << (kb - 64);
+      ++lv.n;
+    }
+  }
+  return lv;
+}
+
+__device__ __forceinline__ bool is_live(const Live& lv, int kb) {
+  return lv.all || (((kb < 64 ? lv.lo >> kb : lv.hi >> (kb - 64)) & 1ull) != 0);
+}
+
 // ------------------------------------------------------------- epilogue ---
 // Drain this warp's RUN accumulator columns into the running sums (round to
 // nearest).  Columns: ch*RUN.. of the tile, except for 128-wide stage-2
@@ -512,7 +564,9 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
         const int bz = p.stage == 1 ? w.q : matrix_slot(p, w.lam);
         const int ay = (2 * w.tm + (int)rank) * BM;
         const int by = w.tn * BN + (int)rank * (tile_n<BN>(p, w.tn) >> 1);
-        for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
+        const Live lv = live_kblocks<BN>(p, w);
+        for (int kb = 0; kb < p.kblocks; ++kb) {
+          if (!is_live(lv, kb)) continue;
           const int s = it % STAGES;
           if (!mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1, p.err)) { ok = false; break; }
           const uint32_t fb = map_to_cta(full_bar(s), 0);
@@ -522,6 +576,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
           tma_load_3d(sa + A_BYTES, &tmA_lo, fb, kb * BK, ay, az);
           tma_load_3d(sa + 2 * A_BYTES, &tmB_hi, fb, kb * BK, by, bz);
           tma_load_3d(sa + 2 * A_BYTES + B_BYTES, &tmB_lo, fb, kb * BK, by, bz);
+          ++it;
         }
       }
       // every copy of both CTAs has landed before the pair exits (the even
@@ -537,12 +592,16 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
       uint32_t gi = 0;                       // accumulator groups issued (accumulator uses)
       bool ok = true;
       for (int i = pair; ok && i < p.n_items; i += npairs) {
+        const Item w = decode(p, i);
         const uint32_t idesc = (p.idesc & ~(0x3Fu << 17)) |
-                               ((uint32_t)(tile_n<BN>(p, decode(p, i).tn) >> 3) << 17);
-        for (int kb = 0; kb < p.kblocks; ++kb, ++it) {
+                               ((uint32_t)(tile_n<BN>(p, w.tn) >> 3) << 17);
+        const Live lv = live_kblocks<BN>(p, w);
+        int j = 0;                           // live K blocks of this item issued
+        for (int kb = 0; kb < p.kblocks; ++kb) {
+          if (!is_live(lv, kb)) continue;
           const int s = it % STAGES, xb = gi & 1;
-          const bool first = kb % Drain<BF16>::KB == 0;
-          const bool last = kb % Drain<BF16>::KB == Drain<BF16>::KB - 1 || kb == p.kblocks - 1;
+          const bool first = j % Drain<BF16>::KB == 0;
+          const bool last = j % Drain<BF16>::KB == Drain<BF16>::KB - 1 || j == lv.n - 1;
           if (!mbar_wait(full_bar(s), (it / STAGES) & 1, p.err)) { ok = false; break; }
           // accumulator xb was drained by both CTAs (its previous group, gi - 2)
           if (first && !mbar_wait(acc_empty(xb), ((gi >> 1) & 1) ^ 1, p.err)) { ok = false; break; }
@@ -563,6 +622,8 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
             mma_commit_pair(acc_full(xb));       // accumulator xb ready for the epilogues
             ++gi;
           }
+          ++j;
+          ++it;
         }
       }
       // all issued MMAs have retired before TMEM is released
@@ -579,9 +640,11 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
     uint8_t* const stg = gbase + STAGES * STAGE_BYTES + (warp - 2) * STG_BYTES;
     uint32_t gi = 0;                         // accumulator groups drained
     bool ok = true;
-    const int groups = (p.kblocks + Drain<BF16>::KB - 1) / Drain<BF16>::KB;
     for (int i = pair; ok && i < p.n_items; i += npairs) {
       Item w = decode(p, i);
+      // accumulator groups of the item (none when its field tile is zero:
+      // the output tile is then written as zeros)
+      const int groups = (live_kblocks<BN>(p, w).n + Drain<BF16>::KB - 1) / Drain<BF16>::KB;
       w.tm = 2 * w.tm + (int)rank;           // this CTA's 128-row tile
       float run[C::RUN];
 #pragma unroll
@@ -803,11 +866,19 @@ static int run_split_mft(const SplitMftProblem& q, cudaEvent_t* ev, cudaStream_t
   p.maxabs = q.maxabs;
   p.err = q.err;
   p.lam_idx = q.lam_idx;
+  if (q.kflags && q.kp1 / 32 <= 128) {         // Live tracks up to 128 K blocks
+    LGB_REQUIRE(q.kf_pitch % 8 == 0 && q.kf_pitch >= kflag_pitch(q.kp2), LGB_EINVAL,
+                "split mft: field flag rows too short for the column tiles");
+    p.kflags = q.kflags;
+    p.kf_units = q.kp1 / 32;
+    p.kf_pitch = q.kf_pitch;
+  }
   if (ev) LGB_CUDA(cudaEventRecord(ev[0], s));
   if ((st = launch_stage<BN>(p, q.bf16, m1, s))) return st;
   if (ev) LGB_CUDA(cudaEventRecord(ev[1], s));
 
   p.stage = 2;
+  p.kflags = nullptr;                           // G is dense
   p.kblocks = sh[1].kblocks;
   p.m_tiles = cdiv(q.M, 2 * BM);
   p.n_tiles = cdiv(q.N, BN / 2);                        // BN/2 complex columns per tile

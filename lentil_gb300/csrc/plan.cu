@@ -238,6 +238,8 @@ struct SplitOperands {
   uint16_t *fh = nullptr, *fl = nullptr, *gh = nullptr, *gl = nullptr;
   float* wbuf = nullptr;
   int ldw = 0;
+  uint8_t* kflags = nullptr;       // [B][kp1/32][kf_pitch] field nonzero flags
+  int kf_pitch = 0;
 };
 
 static size_t carve_operands(void* base, const lgb_psf_desc& d, int kp1, int kp2, int B, int L,
@@ -253,6 +255,8 @@ static size_t carve_operands(void* base, const lgb_psf_desc& d, int kp1, int kp2
   t.gl = c.take<uint16_t>(Q * d.M * 2 * kp2);
   t.ldw = round_up(d.N, 4);
   t.wbuf = c.take<float>((size_t)B * d.M * t.ldw);
+  t.kf_pitch = kflag_pitch(kp2);
+  t.kflags = c.take<uint8_t>((size_t)B * (kp1 / 32) * t.kf_pitch);
   if (o) *o = t;
   return c.used;
 }
@@ -452,6 +456,7 @@ static int psf_execute_n(lgb_psf_plan P, int B, const int* lam_idx, int n_sel, c
     fa.maxabs = ops.maxabs;
     fa.hi = ops.fh; fa.lo = ops.fl;
     fa.lam_idx = lam_idx;
+    fa.kflags = ops.kflags; fa.kf_pitch = ops.kf_pitch;
     if ((st = prof_begin(P, LGB_PROFILE_PHASOR, s, ev))) return st;
     if ((st = launch_split_field_T(fa, bf16, s))) return st;
     if ((st = prof_end(P, LGB_PROFILE_PHASOR, s, ev))) return st;
@@ -470,6 +475,7 @@ static int psf_execute_n(lgb_psf_plan P, int B, const int* lam_idx, int n_sel, c
     p.ldw = ops.ldw;
     p.err = errp;
     p.tile = P->tile;
+    p.kflags = ops.kflags; p.kf_pitch = ops.kf_pitch;   // skip all-zero field blocks
     LGB_CUDA(cudaMemsetAsync(ops.wbuf, 0, sizeof(float) * (size_t)B * d.M * ops.ldw, s));
     cudaEvent_t mev[4];
     if (P->profile) {

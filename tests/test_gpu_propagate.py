@@ -294,3 +294,25 @@ def test_tilt_planes_golden(golden, cuda_device, name, precision, tol):
         budget += wt * w.intensity.max()
     ref = g[f'img_{name}']
     assert lo.peak_normalised_error(img, ref) < tol * budget / ref.max()
+
+
+@pytest.mark.parametrize('tile', [256, 128])
+def test_zero_field_blocks_are_skipped_exactly(cuda_device, tile):
+    # Two discs 870 columns apart: the field's bounding box (671 x 991) holds
+    # whole column tiles without a nonzero entry and many all-zero 64-row K
+    # blocks, which the tensor-core stage 1 skips (an odd count of 21 K
+    # blocks, so one block straddles the real and imaginary rows).  The
+    # result must match the complex128 oracle as a dense field does.
+    H = 1024
+    amp = lg.circle((H, H), 60, shift=(-300, -440)) + lg.circle((H, H), 60, shift=(250, 430))
+    amp = lo.normalize_power(amp)
+    opd = lo.zernike_compose(amp > 0, [0, 0, 0, 80e-9, 30e-9, -20e-9])
+    wl = np.array([600e-9, 700e-9, 800e-9])
+    wt = np.array([0.3, 0.3, 0.4])
+    kw = dict(pixelscale=5e-6, shape=64, oversample=2)
+    ref = lo.broadband_psf(lo.Pupil(amplitude=amp, opd=opd, pixelscale=1 / H, focal_length=10),
+                           wl, wt, **kw)
+    pl = lg.Pupil(amplitude=amp, opd=opd, pixelscale=1 / H, focal_length=10)
+    with lg.tuner.forced(tile):
+        img = lg.broadband_psf(pl, wl, wt, precision='split-bf16', **kw)
+    assert lo.peak_normalised_error(img, ref) < 2e-6
