@@ -90,7 +90,8 @@ def plan_bytes_estimate(plane_shape, fslice, window, L, batch, precision):
     kp1, kp2 = ru(m, 32), ru(n, 32)
     e = L * ((ru(M, 64) // 64 * 128) * 2 * kp1 + (ru(N, 128) // 128 * 256) * 2 * kp2) * 4
     ops = batch * L * (n * 2 * kp1 + M * 2 * kp2) * 4 + batch * M * ru(N, 4) * 4
-    return e + ops
+    flags = batch * (kp1 // 32) * 8 * ((kp2 + 255) // 256)    # field nonzero flags
+    return e + ops + flags
 
 
 class _Buffers:
