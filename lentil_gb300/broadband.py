@@ -17,6 +17,7 @@ propagated field by field through ``propagate_dft`` (same kernels, one
 launch sequence per field) and overlap-added on the device.
 """
 import ctypes
+import threading
 
 import numpy as np
 import torch
@@ -324,16 +325,21 @@ def _deliver(img, out, tensor_io):
 
 
 _PLANS = {}
+_PLANS_LOCK = threading.Lock()
 
 
 def _cached_plan(geo, precision, batch=1):
+    """The PSF plan of a geometry, from an 8-entry FIFO shared by the
+    process's threads (a plan evicted while another thread still uses it
+    lives until that thread drops it)."""
     key = (geo.plane_shape, geo.fslice, tuple(geo.offset), tuple(geo.wavelengths.tolist()),
            tuple(geo.alphas), tuple(geo.shifts), geo.window_shape, geo.shape_out,
            geo.window_origin, precision, batch)
-    p = _PLANS.get(key)
-    if p is None:
-        if len(_PLANS) >= 8:
-            _PLANS.pop(next(iter(_PLANS)))
-        p = make_plan(geo, batch=batch, precision=precision)
-        _PLANS[key] = p
+    with _PLANS_LOCK:
+        p = _PLANS.get(key)
+        if p is None:
+            if len(_PLANS) >= 8:
+                _PLANS.pop(next(iter(_PLANS)))
+            p = make_plan(geo, batch=batch, precision=precision)
+            _PLANS[key] = p
     return p
