@@ -227,7 +227,10 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
   // that minimises whole waves times the work of one block (the last wave
   // of a launch is otherwise partly empty), among counts up to 16.  A
   // block's fixed part (loading amp and opd, the flags) counts as two
-  // wavelengths of work.
+  // wavelengths of work.  A block takes at most 16 wavelengths (when 16
+  // groups allow it), so that no block holds an SM for long: the MFT's
+  // persistent CTA pairs of a launch on another stream start only where an
+  // SM is free, and a late pair delays its whole launch.
   int per_sm = 0;
   auto kfn = bf16 ? (a.amp ? split_field_T_kernel<true, true> : split_field_T_kernel<true, false>)
                   : (a.amp ? split_field_T_kernel<false, true> : split_field_T_kernel<false, false>);
@@ -237,7 +240,8 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
   const long long base = std::max(1LL, (long long)spatial * psfs);
   int groups = 1;
   double best = 1e300;
-  for (int g = 1; g <= std::min(L, 16); ++g) {
+  LGB_REQUIRE(L >= 1, LGB_EINVAL, "split field: no wavelengths");
+  for (int g = std::max(1, std::min(cdiv(L, 16), 16)); g <= std::min(L, 16); ++g) {
     const long long waves = (base * g + cap - 1) / cap;
     const double cost = (double)waves * (double)(cdiv(L, g) + 2);   // waves x work per block
     if (cost < best * (1.0 - 1e-9)) { best = cost; groups = g; }
