@@ -118,7 +118,8 @@ def run_reference(args):
     t_psf = statistics.mean(per) * len(wl.wavelengths)
     value = 1.0 / t_psf
     cores = os.cpu_count()
-    line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': 0,
+    line = {'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT,
+            'n_gpus': args.gpus, 'device': 'host CPU cores (the arm uses no GPU)',
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * t_psf,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
             'data': 'synthetic', 'config': config_dict(wl, args),
