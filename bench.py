@@ -398,11 +398,22 @@ def run_gpu(args):
     pk, pk_kind = peaks()
     peak = pk.get('bf16_tflops_sustained', pk.get('bf16_tflops'))
     achieved = (flops_stage1 + flops_stage2) * args.steps / (mft_ms / 1e3) / 1e12
+    # stage 1 issues only the K blocks whose field rows are nonzero somewhere
+    # in the column tile (the tile width of the timed launches)
+    r0, c0 = geo.fslice[0], geo.fslice[1]
+    width = lg.tuner.last_tile() or 256
+    live = stage1_live_fraction(amp_eff[r0:r0 + m, c0:c0 + n] != 0, width) \
+        if args.precision != 'fp64' else 1.0
+    issued = 3 * (flops_stage1 * live + flops_stage2) * args.steps / (mft_ms / 1e3) / 1e12
     tr = traffic_per_launch()
     roofline = {'bound': 'tensor', 'kernel': 'split_mft_kernel (tcgen05, both MFT stages)',
                 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s', 'frac': achieved / peak,
                 'peak_kind': f'{pk_kind} bf16 dense, sustained',
-                'issued_tflops': 3 * achieved,
+                'issued_tflops': issued,
+                'issued_note': 'three split products per algorithmic flop; stage 1 counts '
+                               'its issued K blocks only (stage1_live_fraction); padding '
+                               'not counted',
+                'stage1_live_fraction': live,
                 'traffic': tr.get('traffic_bytes_per_launch') if tr else None,
                 'traffic_note': tr.get('note') if tr else 'no ncu capture committed',
                 'launches': launches, 'avg_launch_ms': mft_ms / max(1, launches),
@@ -787,6 +798,30 @@ def run_large(args):
                              'kind': 'port', 'sample': '1 of 32 wavelengths through the oracle '
                                                        'loop, extrapolated (pixelate excluded)'}}
     print(json.dumps(line), flush=True)
+
+
+def stage1_live_fraction(field_nonzero, width):
+    """Fraction of the tensor-core stage 1's K blocks that are issued for a
+    field (m x n nonzero pattern) at pair-tile width ``width``: a 64-wide K
+    block covers two 32-row units of the field (the real rows, then the
+    imaginary rows) and is skipped when both are zero across the whole
+    column tile.  1.0 where the kernel tracks no flags (more than 128 K
+    blocks)."""
+    f = np.asarray(field_nonzero, dtype=bool)
+    m, n = f.shape
+    kp1, kp2 = -(-m // 32) * 32, -(-n // 32) * 32
+    units = kp1 // 32                          # == K blocks of stage 1
+    if units > 128:
+        return 1.0
+    g = np.zeros((kp1, kp2), dtype=bool)
+    g[:m, :n] = f
+    k = np.arange(units)
+    tiles = -(-kp2 // width)
+    live = 0
+    for t in range(tiles):
+        u = g[:, t * width:(t + 1) * width].reshape(units, 32, -1).any(axis=(1, 2))
+        live += int(np.count_nonzero(u[(2 * k) % units] | u[(2 * k + 1) % units]))
+    return live / (tiles * units)
 
 
 def tuner_summary(args):
