@@ -45,6 +45,13 @@ typedef void* lgb_stream;                   /* == cudaStream_t */
 const char* lgb_last_error(void);
 /* ABI version, (major << 16) | minor. */
 int lgb_version(void);
+/* Usage of a device's default stream-ordered memory pool, the pool that
+ * entries given no workspace take temporary memory from (the FP64 GEMMs'
+ * split-K partials): out[0..3] = reserved bytes now, reserved high-water
+ * mark, used bytes now, used high-water mark.  reset_high != 0 resets both
+ * high-water marks to the current values first.  A diagnostic; lentil has
+ * no counterpart. */
+int lgb_mempool_usage(int device, int reset_high, unsigned long long out[4]);
 
 /* ------------------------------------------------------------------------
  * DFT matrices.  Replaces lentil/fourier.py:106-110 (_dft2_matrices, with
@@ -130,7 +137,10 @@ int lgb_dft2_plan_destroy(lgb_dft2_plan plan);
  * library (LGB_NOALLOC_SCRATCH_BYTES, held by every GPU that loads it) and
  * the caller passes only f and F.  Transforms needing more scratch than that
  * (lgb_dft2_workspace_size(m, n, M, N, LGB_FP64) bytes) are rejected with
- * LGB_EINVAL.  The first call on a device looks the array's address up with
+ * LGB_EINVAL.  The GEMMs' split-K partial products also live in the array,
+ * after that workspace: a transform whose partials do not fit splits K less
+ * (or not at all), so the call never allocates device memory, not even from
+ * the stream-ordered pool.  The first call on a device looks the array's address up with
  * cudaGetSymbolAddress; make it outside any stream capture.  All calls share
  * the array: calls that overlap on the GPU race.
  * ---------------------------------------------------------------------- */

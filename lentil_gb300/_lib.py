@@ -34,6 +34,7 @@ class PsfDesc(ctypes.Structure):
 SIGNATURES = {
     'lgb_last_error': (ctypes.c_char_p, []),
     'lgb_version': (c_int, []),
+    'lgb_mempool_usage': (c_int, [c_int, c_int, ctypes.POINTER(ctypes.c_ulonglong)]),
     'lgb_dft2_matrices': (c_int, [c_int, c_int, c_int, c_int, c_double, c_double, c_double,
                                   c_double, c_double, c_double, c_void_p, c_void_p, c_void_p]),
     'lgb_dft2_workspace_size': (c_size_t, [c_int, c_int, c_int, c_int, c_int]),

@@ -87,3 +87,22 @@ int make_phase_axis(double alpha, double shift, double offset, int len_in, int l
 
 extern "C" const char* lgb_last_error(void) { return lgb::g_last_error.c_str(); }
 extern "C" int lgb_version(void) { return (1 << 16) | 0; }
+
+extern "C" int lgb_mempool_usage(int device, int reset_high, unsigned long long out[4]) {
+  LGB_REQUIRE(out, LGB_EINVAL, "mempool_usage: null output");
+  cudaMemPool_t pool;
+  LGB_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+  if (reset_high) {
+    unsigned long long zero = 0;
+    LGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReservedMemHigh, &zero));
+    LGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero));
+  }
+  const cudaMemPoolAttr attrs[4] = {cudaMemPoolAttrReservedMemCurrent, cudaMemPoolAttrReservedMemHigh,
+                                    cudaMemPoolAttrUsedMemCurrent, cudaMemPoolAttrUsedMemHigh};
+  for (int i = 0; i < 4; ++i) {
+    unsigned long long v = 0;
+    LGB_CUDA(cudaMemPoolGetAttribute(pool, attrs[i], &v));
+    out[i] = (unsigned long long)v;
+  }
+  return LGB_OK;
+}

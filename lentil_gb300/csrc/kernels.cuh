@@ -56,11 +56,25 @@ int launch_maxabs_c128_batch(const double2* f, int count, int batch, float* out,
 int launch_conj_scale(const double2* in, double2* out, size_t count, double scale, cudaStream_t s);
 
 // mft_fp64.cu ------------------------------------------------------------
+// Caller-provided memory for launch_zgemm's split-K partial products.  With
+// one given, launch_zgemm never allocates: it splits K only as far as the
+// partials fit in `bytes` (not at all when even two splits do not fit).
+struct ZgemmScratch {
+  void* ptr;
+  size_t bytes;
+};
 // C[b] = alpha * A[b] . B[b] (complex128), row-major with leading dims and
-// batch strides (elements).  beta == 0 overwrites C.
+// batch strides (elements).  beta == 0 overwrites C.  Without `scratch`, the
+// split-K partials come from the device's stream-ordered pool.
 int launch_zgemm(int M, int N, int K, const double2* A, int lda, long long sA,
                  const double2* B, int ldb, long long sB, double2* C, int ldc, long long sC,
-                 int batch, double alpha, cudaStream_t s);
+                 int batch, double alpha, cudaStream_t s, const ZgemmScratch* scratch = nullptr);
+// lgb_dft2_batch's body (plan.cu), with the FP64 GEMMs' split-K partials
+// taken from `zs` when it is given (nothing is allocated then)
+int dft2_batch(const double2* f, int count, int m, int n, double2* F, int M, int N,
+               double alpha_r, double alpha_c, double shift_r, double shift_c, double offset_r,
+               double offset_c, int unitary, int precision, void* workspace,
+               size_t workspace_bytes, cudaStream_t s, const ZgemmScratch* zs);
 // out[b] += sum_l weights[b][l] * unit2[l] * |F[b][l]|^2 into a window (FP64)
 int launch_intensity_accum_c128(const double2* F, int M, int N, long long sF, int batch_inner,
                                 const double* weights, const double* unit2, double* out,

@@ -118,11 +118,11 @@ static void keep_pool_memory() {
 // A launch of fewer tiles than SMs would leave the FP64 pipes of most SMs
 // idle (a 256 x 256 output is 16 tiles; each SM retires about two FP64 FMAs
 // a clock), so such a launch splits K over up to 16 CTAs per tile, each
-// writing a partial product to stream-ordered scratch, and a second kernel
-// sums the partials in split order.
+// writing a partial product to scratch (the caller's, or stream-ordered pool
+// memory), and a second kernel sums the partials in split order.
 int launch_zgemm(int M, int N, int K, const double2* A, int lda, long long sA, const double2* B,
                  int ldb, long long sB, double2* C, int ldc, long long sC, int batch, double alpha,
-                 cudaStream_t s) {
+                 cudaStream_t s, const ZgemmScratch* scratch) {
   if (M <= 0 || N <= 0 || batch <= 0) return LGB_OK;
   LGB_REQUIRE(batch <= 65535, LGB_EINVAL, "zgemm: batch too large");
   const long long tiles = (long long)cdiv(N, ZBN) * cdiv(M, ZBM) * batch;
@@ -132,7 +132,13 @@ int launch_zgemm(int M, int N, int K, const double2* A, int lda, long long sA, c
     splits = (int)std::min<long long>({(2LL * sms + tiles - 1) / tiles, (long long)cdiv(K, 2 * ZBK), 16LL,
                                        65535LL / batch});
   const long long sP = (long long)batch * M * N;          // one split's partials
-  if (splits > 1 && (size_t)splits * sP * sizeof(double2) > ((size_t)256 << 20)) splits = 1;
+  const size_t part_bytes = (size_t)sP * sizeof(double2);
+  if (scratch) {                                          // as many splits as fit
+    const size_t fit = scratch->ptr ? scratch->bytes / part_bytes : 0;
+    if ((size_t)splits > fit) splits = (int)fit;
+  } else if (splits > 1 && (size_t)splits * part_bytes > ((size_t)256 << 20)) {
+    splits = 1;
+  }
   if (splits <= 1) {
     dim3 grid(cdiv(N, ZBN), cdiv(M, ZBM), batch);
     zgemm_kernel<<<grid, 256, 0, s>>>(M, N, K, A, lda, sA, B, ldb, sB, C, ldc, sC, alpha, 1, K, 0);
@@ -141,9 +147,13 @@ int launch_zgemm(int M, int N, int K, const double2* A, int lda, long long sA, c
   }
   const int kchunk = round_up(cdiv(K, splits), ZBK);
   splits = cdiv(K, kchunk);
-  keep_pool_memory();
   double2* P = nullptr;
-  LGB_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&P), (size_t)splits * sP * sizeof(double2), s));
+  if (scratch) {
+    P = static_cast<double2*>(scratch->ptr);
+  } else {
+    keep_pool_memory();
+    LGB_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&P), (size_t)splits * part_bytes, s));
+  }
   dim3 grid(cdiv(N, ZBN), cdiv(M, ZBM), batch * splits);
   zgemm_kernel<<<grid, 256, 0, s>>>(M, N, K, A, lda, sA, B, ldb, sB, P, N, (long long)M * N, 1.0,
                                     splits, kchunk, sP);
@@ -153,7 +163,7 @@ int launch_zgemm(int M, int N, int K, const double2* A, int lda, long long sA, c
     zgemm_reduce_kernel<<<rgrid, 128, 0, s>>>(P, splits, sP, M, N, C, ldc, sC, alpha);
     e = cudaGetLastError();
   }
-  cudaFreeAsync(P, s);
+  if (!scratch) cudaFreeAsync(P, s);
   LGB_CUDA(e);
   return LGB_OK;
 }

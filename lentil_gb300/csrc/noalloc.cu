@@ -19,10 +19,16 @@
 // ordering between them) race on it.  Nothing in it needs to start at zero:
 // the transform overwrites every scratch element it reads, and the status word
 // at its start is cleared by each call.
+//
+// The plain FP64 GEMMs split K over several CTAs when the output has fewer
+// tiles than the GPU has SMs; their partial products go to the part of the
+// array after the transform's workspace (fewer splits when they do not fit),
+// never to freshly allocated memory.
 #include <mutex>
 #include <vector>
 
 #include "common.cuh"
+#include "kernels.cuh"
 
 namespace lgb {
 
@@ -63,6 +69,10 @@ extern "C" int lgb_dft2_noalloc(const lgb_c128* f, int m, int n, lgb_c128* F, in
   void* ws = nullptr;
   int st = scratch_address(&ws);
   if (st) return st;
-  return lgb_dft2(f, m, n, F, M, N, alpha_r, alpha_c, shift_r, shift_c, offset_r, offset_c,
-                  unitary, LGB_FP64, ws, need, stream);
+  const size_t part_off = align_up(need, 256);
+  ZgemmScratch partials{static_cast<unsigned char*>(ws) + part_off,
+                        (size_t)LGB_NOALLOC_SCRATCH_BYTES - part_off};
+  return dft2_batch(reinterpret_cast<const double2*>(f), 1, m, n, reinterpret_cast<double2*>(F),
+                    M, N, alpha_r, alpha_c, shift_r, shift_c, offset_r, offset_c, unitary,
+                    LGB_FP64, ws, need, as_stream(stream), &partials);
 }

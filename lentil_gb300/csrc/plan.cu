@@ -104,10 +104,20 @@ extern "C" int lgb_dft2_batch(const lgb_c128* f, int count, int m, int n, lgb_c1
                               int precision, void* workspace, size_t workspace_bytes,
                               lgb_stream stream) {
   LGB_RANGE("lgb_dft2_batch");
+  return dft2_batch(reinterpret_cast<const double2*>(f), count, m, n,
+                    reinterpret_cast<double2*>(F), M, N, alpha_r, alpha_c, shift_r, shift_c,
+                    offset_r, offset_c, unitary, precision, workspace, workspace_bytes,
+                    as_stream(stream), nullptr);
+}
+
+int lgb::dft2_batch(const double2* fin, int count, int m, int n, double2* Fout, int M, int N,
+                    double alpha_r, double alpha_c, double shift_r, double shift_c,
+                    double offset_r, double offset_c, int unitary, int precision, void* workspace,
+                    size_t workspace_bytes, cudaStream_t s, const ZgemmScratch* zs) {
   int st = check_sizes(m, n, M, N);
   if (st) return st;
   LGB_REQUIRE(count >= 1 && count <= 65535, LGB_EINVAL, "dft2: count outside 1..65535");
-  LGB_REQUIRE(f && F, LGB_EINVAL, "dft2: null input or output");
+  LGB_REQUIRE(fin && Fout, LGB_EINVAL, "dft2: null input or output");
   LGB_REQUIRE(precision == LGB_FP64 || is_split(precision), LGB_EINVAL, "dft2: unknown precision");
   LGB_REQUIRE(workspace && ((uintptr_t)workspace & 255) == 0, LGB_EWORKSPACE,
               "dft2: workspace must be non-null and 256-byte aligned");
@@ -117,9 +127,6 @@ extern "C" int lgb_dft2_batch(const lgb_c128* f, int count, int m, int n, lgb_c1
   if ((st = make_phase_axis(alpha_r, shift_r, offset_r, m, M, &ar))) return st;
   if ((st = make_phase_axis(alpha_c, shift_c, offset_c, n, N, &ac))) return st;
   const double scale = unitary ? std::sqrt(std::fabs(alpha_r * alpha_c)) : 1.0;
-  cudaStream_t s = as_stream(stream);
-  const double2* fin = reinterpret_cast<const double2*>(f);
-  double2* Fout = reinterpret_cast<double2*>(F);
 
   if (precision == LGB_FP64) {
     Dft2Fp64Space w;
@@ -134,12 +141,12 @@ extern "C" int lgb_dft2_batch(const lgb_c128* f, int count, int m, int n, lgb_c1
     const double cost_right = (double)m * n * N + (double)M * m * N;
     if (cost_left <= cost_right) {
       const long long sT = (long long)M * n;
-      if ((st = launch_zgemm(M, n, m, w.E1, m, 0, fin, n, sf, w.T, n, sT, count, 1.0, s))) return st;
-      return launch_zgemm(M, N, n, w.T, n, sT, w.E2, N, 0, Fout, N, sF, count, scale, s);
+      if ((st = launch_zgemm(M, n, m, w.E1, m, 0, fin, n, sf, w.T, n, sT, count, 1.0, s, zs))) return st;
+      return launch_zgemm(M, N, n, w.T, n, sT, w.E2, N, 0, Fout, N, sF, count, scale, s, zs);
     }
     const long long sT = (long long)m * N;
-    if ((st = launch_zgemm(m, N, n, fin, n, sf, w.E2, N, 0, w.T, N, sT, count, 1.0, s))) return st;
-    return launch_zgemm(M, N, m, w.E1, m, 0, w.T, N, sT, Fout, N, sF, count, scale, s);
+    if ((st = launch_zgemm(m, N, n, fin, n, sf, w.E2, N, 0, w.T, N, sT, count, 1.0, s, zs))) return st;
+    return launch_zgemm(M, N, m, w.E1, m, 0, w.T, N, sT, Fout, N, sF, count, scale, s, zs);
   }
 
   // split precision on the tensor cores: one launch pair for the whole batch
