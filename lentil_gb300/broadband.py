@@ -121,6 +121,16 @@ class PSFPlan:
         _lib.check(lib.lgb_psf_plan_create(ctypes.byref(d), ctypes.byref(h), dv.stream_ptr()))
         self._h = h
         self.nbytes = lib.lgb_psf_plan_bytes(h)
+        # executes without a caller workspace share the plan's own operand
+        # buffers and status word: they are issued one at a time (lock) and
+        # each waits on the device for the previous one (event), whatever
+        # stream or thread it comes from
+        self._own_lock = threading.Lock()
+        self._own_done = None
+        # the DFT matrices are built on the creating stream; executes on any
+        # other stream wait for them on the device
+        self._built = torch.cuda.Event()
+        self._built.record(torch.cuda.current_stream())
 
     def __del__(self):
         h = getattr(self, '_h', None)
@@ -171,6 +181,8 @@ class PSFPlan:
         if out is None:
             out = torch.empty((count,) + self.image_shape, dtype=torch.float64, device=dev)
             accumulate = False
+        if not torch.cuda.is_current_stream_capturing():
+            torch.cuda.current_stream().wait_event(self._built)
         if workspace is not None:
             if lam_idx is not None and (lam_idx.dtype != torch.int32 or not lam_idx.is_cuda):
                 raise TypeError('lam_idx must be an int32 CUDA tensor')
@@ -181,17 +193,26 @@ class PSFPlan:
             if check:
                 _lib.call('lgb_dft2_status', workspace.data_ptr(), dv.stream_ptr())
             return out
-        if lam_idx is None:
-            _lib.call('lgb_psf_execute_batch', self._h, count, amp.data_ptr(), opd.data_ptr(),
-                      weights.data_ptr(), out.data_ptr(), int(bool(accumulate)), dv.stream_ptr())
-        else:
-            if lam_idx.dtype != torch.int32 or not lam_idx.is_cuda:
-                raise TypeError('lam_idx must be an int32 CUDA tensor')
-            _lib.call('lgb_psf_execute_subset', self._h, count, lam_idx.data_ptr(), n_sel,
-                      amp.data_ptr(), opd.data_ptr(), weights.data_ptr(), out.data_ptr(),
-                      int(bool(accumulate)), dv.stream_ptr())
-        if check:
-            _lib.call('lgb_psf_plan_status', self._h, dv.stream_ptr())
+        if lam_idx is not None and (lam_idx.dtype != torch.int32 or not lam_idx.is_cuda):
+            raise TypeError('lam_idx must be an int32 CUDA tensor')
+        with self._own_lock:
+            cur = torch.cuda.current_stream()
+            capturing = torch.cuda.is_current_stream_capturing()
+            if self._own_done is not None and not capturing:
+                cur.wait_event(self._own_done)
+            if lam_idx is None:
+                _lib.call('lgb_psf_execute_batch', self._h, count, amp.data_ptr(),
+                          opd.data_ptr(), weights.data_ptr(), out.data_ptr(),
+                          int(bool(accumulate)), cur.cuda_stream)
+            else:
+                _lib.call('lgb_psf_execute_subset', self._h, count, lam_idx.data_ptr(), n_sel,
+                          amp.data_ptr(), opd.data_ptr(), weights.data_ptr(), out.data_ptr(),
+                          int(bool(accumulate)), cur.cuda_stream)
+            if not capturing:
+                self._own_done = torch.cuda.Event()
+                self._own_done.record(cur)
+            if check:
+                _lib.call('lgb_psf_plan_status', self._h, cur.cuda_stream)
         return out
 
 

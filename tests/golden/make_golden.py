@@ -5,9 +5,10 @@ small ``.npz`` fixtures next to this script.  The reference package cannot
 travel to the GPU machine, so the fixtures are committed and the tests only
 read them.
 
-Usage (in a checkout that has the lentil sources):
+Usage (the argument is the root of a lentil 0.8.8 source tree, the
+directory that holds its ``lentil/`` package):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <lentil-source-root>
 """
 import os
 import sys
@@ -344,4 +345,6 @@ def main(ref_root):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    if len(sys.argv) != 2 or not os.path.isfile(os.path.join(sys.argv[1], 'lentil', '__init__.py')):
+        sys.exit('usage: make_golden.py <lentil-source-root>  (the directory holding lentil/)')
+    main(sys.argv[1])
