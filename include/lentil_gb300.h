@@ -342,6 +342,15 @@ typedef struct {
 } lgb_psf_desc;
 
 int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan, lgb_stream stream);
+/* The same plan in caller-owned device memory of lgb_psf_plan_size(desc)
+ * bytes (256-byte aligned; 0 for an invalid desc), e.g. a block of the
+ * caller's caching allocator, so that building a plan maps no new device
+ * memory once the caller holds a block that size.  lgb_psf_plan_destroy
+ * leaves that memory alone: the caller keeps it alive until the plan's
+ * executes are done. */
+size_t lgb_psf_plan_size(const lgb_psf_desc* desc);
+int lgb_psf_plan_create_in(const lgb_psf_desc* desc, void* memory, size_t memory_bytes,
+                           lgb_psf_plan* plan, lgb_stream stream);
 /* device bytes held by the plan */
 size_t lgb_psf_plan_bytes(lgb_psf_plan plan);
 /* amp, opd: [batch][H][W] float64 (amp already multiplied by the mask);
@@ -394,6 +403,21 @@ int lgb_psf_plan_kernel_times(lgb_psf_plan plan, double* ms, int* launches, int 
 /* Releases the plan's memory (stream-ordered on the creation stream); call
  * it after the plan's last execute has completed. */
 int lgb_psf_plan_destroy(lgb_psf_plan plan);
+
+/* ------------------------------------------------------------------------
+ * Test of the tensor-core MFT's bounded waits (no lentil counterpart).  Every
+ * mbarrier wait of the split-precision kernel is bounded in time; on expiry
+ * the kernel records LGB_ETIMEOUT in the entry's device status word, retires
+ * the copies and MMAs it issued and returns, and the entry's status call
+ * (lgb_dft2_status, lgb_dft2_plan_status, lgb_psf_plan_status) reports it.
+ * This one-shot hook makes the NEXT stage-1 split launch of the process (any
+ * entry, any thread) arrive on the full barrier of K block `kblock` of work
+ * item `item` without issuing that block's loads, so the barrier never
+ * completes, and bounds every wait of that launch by wait_ms (0 < wait_ms
+ * <= 2000) instead of the default 2 s.  The launch then runs out, reports
+ * LGB_ETIMEOUT, and later launches run normally.
+ * ---------------------------------------------------------------------- */
+int lgb_test_stall_tma(int item, int kblock, double wait_ms);
 
 /* ------------------------------------------------------------------------
  * Tile-shape autotuner of the split-precision MFT (extension: lentil has no

@@ -35,6 +35,7 @@ SIGNATURES = {
     'lgb_last_error': (ctypes.c_char_p, []),
     'lgb_version': (c_int, []),
     'lgb_mempool_usage': (c_int, [c_int, c_int, ctypes.POINTER(ctypes.c_ulonglong)]),
+    'lgb_test_stall_tma': (c_int, [c_int, c_int, c_double]),
     'lgb_dft2_matrices': (c_int, [c_int, c_int, c_int, c_int, c_double, c_double, c_double,
                                   c_double, c_double, c_double, c_void_p, c_void_p, c_void_p]),
     'lgb_dft2_workspace_size': (c_size_t, [c_int, c_int, c_int, c_int, c_int]),
@@ -112,6 +113,9 @@ SIGNATURES = {
                                    c_int, c_int, c_void_p]),
     'lgb_psf_plan_create': (c_int, [ctypes.POINTER(PsfDesc), ctypes.POINTER(c_void_p), c_void_p]),
     'lgb_psf_plan_bytes': (c_size_t, [c_void_p]),
+    'lgb_psf_plan_size': (c_size_t, [ctypes.POINTER(PsfDesc)]),
+    'lgb_psf_plan_create_in': (c_int, [ctypes.POINTER(PsfDesc), c_void_p, c_size_t,
+                                       ctypes.POINTER(c_void_p), c_void_p]),
     'lgb_psf_execute': (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     'lgb_psf_execute_batch': (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_int, c_void_p]),

@@ -117,8 +117,19 @@ class PSFPlan:
         d.batch = self.batch
         d.precision = _lib.precision_code(precision)
         self.desc = d
+        # plan memory is a block of torch's caching allocator: a plan built
+        # where an earlier one was released reuses its memory without
+        # mapping new device memory; executes on other streams are recorded
+        # on the block so that it outlives their work
+        nbytes = lib.lgb_psf_plan_size(ctypes.byref(d))
+        if nbytes == 0:
+            _lib.check(lib.lgb_psf_plan_create(ctypes.byref(d), None, None))   # raises the reason
+        self._home = torch.cuda.current_stream()
+        self._foreign = set()
+        self._mem = dv.workspace(nbytes)
         h = ctypes.c_void_p()
-        _lib.check(lib.lgb_psf_plan_create(ctypes.byref(d), ctypes.byref(h), dv.stream_ptr()))
+        _lib.check(lib.lgb_psf_plan_create_in(ctypes.byref(d), self._mem.data_ptr(), nbytes,
+                                              ctypes.byref(h), self._home.cuda_stream))
         self._h = h
         self.nbytes = lib.lgb_psf_plan_bytes(h)
         # executes without a caller workspace share the plan's own operand
@@ -130,7 +141,7 @@ class PSFPlan:
         # the DFT matrices are built on the creating stream; executes on any
         # other stream wait for them on the device
         self._built = torch.cuda.Event()
-        self._built.record(torch.cuda.current_stream())
+        self._built.record(self._home)
 
     def __del__(self):
         h = getattr(self, '_h', None)
@@ -181,8 +192,12 @@ class PSFPlan:
         if out is None:
             out = torch.empty((count,) + self.image_shape, dtype=torch.float64, device=dev)
             accumulate = False
-        if not torch.cuda.is_current_stream_capturing():
-            torch.cuda.current_stream().wait_event(self._built)
+        cur = torch.cuda.current_stream()
+        if cur != self._home and not torch.cuda.is_current_stream_capturing():
+            cur.wait_event(self._built)
+            if cur.cuda_stream not in self._foreign:
+                self._mem.record_stream(cur)
+                self._foreign.add(cur.cuda_stream)
         if workspace is not None:
             if lam_idx is not None and (lam_idx.dtype != torch.int32 or not lam_idx.is_cuda):
                 raise TypeError('lam_idx must be an int32 CUDA tensor')

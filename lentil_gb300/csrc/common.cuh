@@ -94,6 +94,18 @@ __device__ __forceinline__ uint64_t phase_fixed(const PhaseAxis& ax, int i_in, i
   return ph;
 }
 
+// Increment of phase_fixed(ax, i, j) from input index i to i + 1 at output
+// index j: frac(alpha*Y) - frac(alpha*sf) in the same 2^-64-cycle units.  A
+// phase stepped by it agrees with phase_fixed to a few units of 2^-64 cycles
+// (the truncated low half of alpha's 128-bit product).
+__device__ __forceinline__ uint64_t phase_step_in(const PhaseAxis& ax, int j_out) {
+  const int64_t Y = ax.y0 + j_out;
+  const uint64_t Yu = (uint64_t)Y;
+  uint64_t hi = __umul64hi(ax.a_lo, Yu);
+  if (Y < 0) hi -= ax.a_lo;
+  return ax.a_hi * Yu + hi - ax.b_sf;
+}
+
 // exp(-2*pi*i*phase) in double precision from the fixed-point phase.
 __device__ __forceinline__ double2 expm2pi_fixed_f64(uint64_t ph) {
   const double x = (double)(int64_t)ph * 0x1p-63;   // half-cycles in [-1, 1)

@@ -43,66 +43,100 @@ int launch_dft_matrix_c128(const PhaseAxis& ax, int len_in, int len_out, double2
   return LGB_OK;
 }
 
+// Both split builders: a thread makes 4 consecutive K entries of one
+// output row/column.  The phase is taken once in fixed point and stepped by
+// its exact per-index increment; the four values are split in pairs and
+// written as 8-byte stores to the four places a block embedding holds them
+// ([Re | -Im] and [Im | Re] rows).  The negated imaginary part is the split
+// of the imaginary part with the sign bits flipped (round-to-nearest is
+// symmetric, so this equals splitting -Im).
+constexpr int SPLIT_PER_THREAD = 4;
+constexpr int SPLIT_THREADS = 128;
+
+template <bool BF16>
+__device__ __forceinline__ void block_entries_store(const PhaseAxis& ax, int k0, int len_in,
+                                                    int j_out, bool live_row, int kp,
+                                                    size_t row_re, size_t row_im,
+                                                    uint16_t* __restrict__ hi,
+                                                    uint16_t* __restrict__ lo) {
+  float2 e[SPLIT_PER_THREAD];
+  uint64_t ph = phase_fixed(ax, k0, j_out);
+  const uint64_t step = phase_step_in(ax, j_out);
+#pragma unroll
+  for (int t = 0; t < SPLIT_PER_THREAD; ++t) {
+    e[t] = (live_row && k0 + t < len_in) ? expm2pi_fixed_f32(ph) : make_float2(0.f, 0.f);
+    ph += step;
+  }
+  uint32_t rh[2], rl[2], ih[2], il[2];
+#pragma unroll
+  for (int t = 0; t < 2; ++t) {
+    Split16x2<BF16>::split(e[2 * t].x, e[2 * t + 1].x, rh[t], rl[t]);
+    Split16x2<BF16>::split(e[2 * t].y, e[2 * t + 1].y, ih[t], il[t]);
+  }
+  constexpr uint32_t SIGN = 0x80008000u;
+  const uint2 re_h = make_uint2(rh[0], rh[1]), re_l = make_uint2(rl[0], rl[1]);
+  const uint2 im_h = make_uint2(ih[0], ih[1]), im_l = make_uint2(il[0], il[1]);
+  const uint2 nim_h = make_uint2(ih[0] ^ SIGN, ih[1] ^ SIGN);
+  const uint2 nim_l = make_uint2(il[0] ^ SIGN, il[1] ^ SIGN);
+  auto st = [&](uint16_t* base, size_t off, uint2 v) {
+    *reinterpret_cast<uint2*>(base + off) = v;
+  };
+  st(hi, row_re + k0, re_h);       st(lo, row_re + k0, re_l);        // [ Re | . ]
+  st(hi, row_re + kp + k0, nim_h); st(lo, row_re + kp + k0, nim_l);  // [ . | -Im ]
+  st(hi, row_im + k0, im_h);       st(lo, row_im + k0, im_l);        // [ Im | . ]
+  st(hi, row_im + kp + k0, re_h);  st(lo, row_im + kp + k0, re_l);   // [ . | Re ]
+}
+
 // Stage-1 A operand, one wavelength per blockIdx.z.
 template <bool BF16>
-__global__ void e1_block_split_kernel(const PhaseAxis* __restrict__ axes, int m, int M, int kp,
-                                      int rows_padded, uint16_t* __restrict__ hi,
-                                      uint16_t* __restrict__ lo) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;    // input row index (K)
+__global__ void __launch_bounds__(SPLIT_THREADS) e1_block_split_kernel(
+    const PhaseAxis* __restrict__ axes, int m, int M, int kp, int rows_padded,
+    uint16_t* __restrict__ hi, uint16_t* __restrict__ lo) {
+  const int r0 = SPLIT_PER_THREAD * (blockIdx.x * blockDim.x + threadIdx.x);   // K index
   const int u = blockIdx.y;                                // output row
   const int z = blockIdx.z;
-  if (r >= kp) return;
-  float2 e = make_float2(0.f, 0.f);
-  if (r < m && u < M) e = expm2pi_fixed_f32(phase_fixed(axes[z], r, u));
+  if (r0 >= kp) return;
   const int t = u >> 6, i = u & 63;
   const size_t K = 2 * (size_t)kp;
   const size_t base = (size_t)z * rows_padded * K;
-  const size_t row_re = base + (size_t)(t * 128 + i) * K;
-  const size_t row_im = base + (size_t)(t * 128 + 64 + i) * K;
-  uint16_t h, l;
-  Split16<BF16>::split(e.x, h, l);  hi[row_re + r] = h;      lo[row_re + r] = l;
-                                    hi[row_im + kp + r] = h; lo[row_im + kp + r] = l;
-  Split16<BF16>::split(-e.y, h, l); hi[row_re + kp + r] = h; lo[row_re + kp + r] = l;
-  Split16<BF16>::split(e.y, h, l);  hi[row_im + r] = h;      lo[row_im + r] = l;
+  block_entries_store<BF16>(axes[z], r0, m, u, u < M, kp, base + (size_t)(t * 128 + i) * K,
+                            base + (size_t)(t * 128 + 64 + i) * K, hi, lo);
 }
 
 // Stage-2 B operand, one wavelength per blockIdx.z.
 template <bool BF16>
-__global__ void e2_block_split_kernel(const PhaseAxis* __restrict__ axes, int n, int N, int kp,
-                                      int rows_padded, uint16_t* __restrict__ hi,
-                                      uint16_t* __restrict__ lo) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;    // intermediate column (K)
+__global__ void __launch_bounds__(SPLIT_THREADS) e2_block_split_kernel(
+    const PhaseAxis* __restrict__ axes, int n, int N, int kp, int rows_padded,
+    uint16_t* __restrict__ hi, uint16_t* __restrict__ lo) {
+  const int c0 = SPLIT_PER_THREAD * (blockIdx.x * blockDim.x + threadIdx.x);   // K index
   const int v = blockIdx.y;                                // output column
   const int z = blockIdx.z;
-  if (c >= kp) return;
-  float2 e = make_float2(0.f, 0.f);
-  if (c < n && v < N) e = expm2pi_fixed_f32(phase_fixed(axes[z], c, v));
+  if (c0 >= kp) return;
   const int t = v >> 7, h2 = (v >> 6) & 1, j = v & 63;
   const size_t K = 2 * (size_t)kp;
   const size_t base = (size_t)z * rows_padded * K;
-  const size_t row_re = base + (size_t)(t * 256 + h2 * 128 + j) * K;
-  const size_t row_im = base + (size_t)(t * 256 + h2 * 128 + 64 + j) * K;
-  uint16_t h, l;
-  Split16<BF16>::split(e.x, h, l);  hi[row_re + c] = h;      lo[row_re + c] = l;
-                                    hi[row_im + kp + c] = h; lo[row_im + kp + c] = l;
-  Split16<BF16>::split(-e.y, h, l); hi[row_re + kp + c] = h; lo[row_re + kp + c] = l;
-  Split16<BF16>::split(e.y, h, l);  hi[row_im + c] = h;      lo[row_im + c] = l;
+  block_entries_store<BF16>(axes[z], c0, n, v, v < N, kp,
+                            base + (size_t)(t * 256 + h2 * 128 + j) * K,
+                            base + (size_t)(t * 256 + h2 * 128 + 64 + j) * K, hi, lo);
 }
 
 int launch_e1_block_split(const PhaseAxis* d_axes, int L, int m, int M, int kp, int rows_padded,
                           bool bf16, uint16_t* hi, uint16_t* lo, cudaStream_t s) {
-  dim3 grid(cdiv(kp, 128), rows_padded / 2, L);   // rows_padded/2 output rows incl. padding
-  if (bf16) e1_block_split_kernel<true><<<grid, 128, 0, s>>>(d_axes, m, M, kp, rows_padded, hi, lo);
-  else e1_block_split_kernel<false><<<grid, 128, 0, s>>>(d_axes, m, M, kp, rows_padded, hi, lo);
+  LGB_REQUIRE(kp % SPLIT_PER_THREAD == 0, LGB_EINVAL, "e1 block: K padding must be a multiple of 4");
+  // rows_padded/2 output rows incl. padding
+  dim3 grid(cdiv(kp, SPLIT_PER_THREAD * SPLIT_THREADS), rows_padded / 2, L);
+  if (bf16) e1_block_split_kernel<true><<<grid, SPLIT_THREADS, 0, s>>>(d_axes, m, M, kp, rows_padded, hi, lo);
+  else e1_block_split_kernel<false><<<grid, SPLIT_THREADS, 0, s>>>(d_axes, m, M, kp, rows_padded, hi, lo);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }
 
 int launch_e2_block_split(const PhaseAxis* d_axes, int L, int n, int N, int kp, int rows_padded,
                           bool bf16, uint16_t* hi, uint16_t* lo, cudaStream_t s) {
-  dim3 grid(cdiv(kp, 128), rows_padded / 2, L);
-  if (bf16) e2_block_split_kernel<true><<<grid, 128, 0, s>>>(d_axes, n, N, kp, rows_padded, hi, lo);
-  else e2_block_split_kernel<false><<<grid, 128, 0, s>>>(d_axes, n, N, kp, rows_padded, hi, lo);
+  LGB_REQUIRE(kp % SPLIT_PER_THREAD == 0, LGB_EINVAL, "e2 block: K padding must be a multiple of 4");
+  dim3 grid(cdiv(kp, SPLIT_PER_THREAD * SPLIT_THREADS), rows_padded / 2, L);
+  if (bf16) e2_block_split_kernel<true><<<grid, SPLIT_THREADS, 0, s>>>(d_axes, n, N, kp, rows_padded, hi, lo);
+  else e2_block_split_kernel<false><<<grid, SPLIT_THREADS, 0, s>>>(d_axes, n, N, kp, rows_padded, hi, lo);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }

@@ -102,15 +102,37 @@ int launch_phasor_batch_c128(const double* amp, const double* opd, int H, int W,
 // wavelengths (blockIdx.x = row tile * groups + group, blockIdx.z = PSF).
 // Splitting the wavelength loop over blocks keeps enough blocks in flight to
 // cover HBM latency; the groups of one tile are adjacent in launch order, so
-// that their re-reads of amp and opd hit L2.  The transpose tile is
-// double-buffered, so each wavelength needs one barrier.
+// that their re-reads of amp and opd hit L2.
+// Per wavelength the block's four output planes (real/imaginary x hi/lo, 32
+// rows of 64 K values = 128 bytes each) are written into shared memory in
+// the 128-byte-swizzled layout of a TMA box and leave as four bulk tensor
+// stores issued by one thread; the TMA clips rows past n and K values past
+// kp.  The tiles are double-buffered, so each wavelength needs one barrier:
+// before it, the issuing thread waits until the previous wavelength's stores
+// have read their tiles, which frees the buffer the next wavelength writes.
 // ---------------------------------------------------------------------------
-constexpr int TR = 64, TC = 32, TPAD = 8;
+constexpr int TR = 64, TC = 32;
+constexpr uint32_t FT_PLANE_BYTES = TC * TR * 2;            // 4 KB: 32 rows x 128 B
+constexpr uint32_t FT_SMEM_BYTES = 2 * 4 * FT_PLANE_BYTES + 1024;   // two buffers + alignment
+
+__device__ __forceinline__ void ft_store_4d(const CUtensorMap* map, uint32_t src, int x, int y,
+                                            int z, int w) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(src), "r"(x), "r"(y), "r"(z), "r"(w)
+      : "memory");
+}
 
 template <bool BF16, bool PHASOR>
-__global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, int groups) {
-  __shared__ __align__(16) uint16_t tile[2][4][TC][TR + TPAD];   // re_hi, re_lo, im_hi, im_lo
+__global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, int groups,
+                                                            const __grid_constant__ CUtensorMap map_hi,
+                                                            const __grid_constant__ CUtensorMap map_lo) {
+  extern __shared__ uint8_t ft_smem_raw[];
   __shared__ int warp_nz[8];
+  const uint32_t raw = (uint32_t)__cvta_generic_to_shared(ft_smem_raw);
+  const uint32_t tiles = (raw + 1023u) & ~1023u;                          // 1024-byte aligned
+  uint8_t* const tile = ft_smem_raw + (tiles - raw);
   const int tid = threadIdx.x;
   const int rtile = blockIdx.x / groups, g = blockIdx.x - rtile * groups;   // row tile, group
   const int rt = rtile * TR, ct = blockIdx.y * TC;
@@ -119,7 +141,8 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
 
   // thread (w, lane) owns field column ct + lane and rows rt + 8w .. 8w+7:
   // each global load instruction reads 32 consecutive columns of one row,
-  // and the thread's 8 values of a plane are one 16-byte shared store
+  // and the thread's 8 values of a plane are one 16-byte chunk of its tile
+  // row (chunk w of row lane, swizzled: no bank conflicts)
   const int lane = tid & 31, w = tid >> 5;
   float amp_r[8], o_hi[8], o_lo[8];
   float2 fv[8];
@@ -165,6 +188,7 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
   const int L = PHASOR ? a.L : 1;
   const int per = (L + groups - 1) / groups;
   const int l0 = g * per, l1 = min(L, l0 + per);
+  const uint32_t chunk = (uint32_t)lane * 128u + ((uint32_t)(w ^ (lane & 7)) << 4);
   for (int l = l0; l < l1; ++l) {
     if (PHASOR) {
       const float2 kk = a.khalf[a.lam_idx ? a.lam_idx[l] : l];   // 2/lambda, float-float pair
@@ -192,28 +216,28 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
       Split16x2<BF16>::split(fv[2 * j].x, fv[2 * j + 1].x, pk[0][j], pk[1][j]);
       Split16x2<BF16>::split(fv[2 * j].y, fv[2 * j + 1].y, pk[2][j], pk[3][j]);
     }
-    // buffer l&1 was last read two wavelengths ago, before the barrier of the
-    // previous wavelength; row pitch 144 B keeps 8 lanes' 16-byte stores on
-    // distinct banks
-    uint16_t (*t)[TC][TR + TPAD] = tile[l & 1];
+    // buffer l&1 was read by the stores of wavelength l-2, which the issuing
+    // thread saw completed before the previous barrier
+    uint8_t* const buf = tile + (l & 1) * 4 * FT_PLANE_BYTES;
 #pragma unroll
-    for (int pl = 0; pl < 4; ++pl)
-      *reinterpret_cast<uint4*>(&t[pl][lane][8 * w]) = make_uint4(pk[pl][0], pk[pl][1], pk[pl][2], pk[pl][3]);
+    for (int pl = 0; pl < 4; ++pl)                   // re_hi, re_lo, im_hi, im_lo
+      *reinterpret_cast<uint4*>(buf + pl * FT_PLANE_BYTES + chunk) =
+          make_uint4(pk[pl][0], pk[pl][1], pk[pl][2], pk[pl][3]);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
     __syncthreads();
-    const size_t q = (size_t)b * L + l;
-    const size_t K = 2 * (size_t)a.kp;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int v = tid + 256 * k;                   // 1024 16-byte vectors
-      const int plane = v >> 8, cl = (v >> 3) & 31, seg = v & 7;
-      const int c = ct + cl, r = rt + seg * 8;
-      if (c < a.n && r < a.kp) {
-        uint16_t* dst = (plane & 1) ? a.lo : a.hi;
-        const size_t off = (q * a.n + c) * K + ((plane >> 1) ? a.kp : 0) + r;
-        *reinterpret_cast<uint4*>(dst + off) = *reinterpret_cast<const uint4*>(&t[plane][cl][seg * 8]);
-      }
+    if (tid == 0) {
+      const uint32_t sb = tiles + (l & 1) * 4 * FT_PLANE_BYTES;
+      const int q = b * L + l;
+      ft_store_4d(&map_hi, sb, rt, 0, ct, q);
+      ft_store_4d(&map_lo, sb + FT_PLANE_BYTES, rt, 0, ct, q);
+      ft_store_4d(&map_hi, sb + 2 * FT_PLANE_BYTES, rt, 1, ct, q);
+      ft_store_4d(&map_lo, sb + 3 * FT_PLANE_BYTES, rt, 1, ct, q);
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
     }
   }
+  // the stores have landed before the block (and its shared memory) ends
+  if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
@@ -222,6 +246,12 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
   const int spatial = cdiv(a.kp, TR) * cdiv(a.n, TC);
   const int psfs = a.batch;
   const int L = a.amp ? a.L : 1;
+  LGB_REQUIRE(L >= 1, LGB_EINVAL, "split field: no wavelengths");
+  LGB_REQUIRE(psfs <= 65535, LGB_EINVAL, "split field: too many PSFs in one launch");
+  CUtensorMap map_hi, map_lo;
+  int st;
+  if ((st = make_field_T_store_map(&map_hi, a.hi, bf16, a.kp, a.n, psfs * L))) return st;
+  if ((st = make_field_T_store_map(&map_lo, a.lo, bf16, a.kp, a.n, psfs * L))) return st;
   // Wavelength groups: each group re-reads the block's amp/opd once, and
   // the blocks run in waves of `cap` resident blocks; pick the group count
   // that minimises whole waves times the work of one block (the last wave
@@ -234,28 +264,21 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
   int per_sm = 0;
   auto kfn = bf16 ? (a.amp ? split_field_T_kernel<true, true> : split_field_T_kernel<true, false>)
                   : (a.amp ? split_field_T_kernel<false, true> : split_field_T_kernel<false, false>);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, 0) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 256, FT_SMEM_BYTES) != cudaSuccess ||
+      per_sm < 1)
     per_sm = 1;
   const long long cap = (long long)per_sm * sm_count();
   const long long base = std::max(1LL, (long long)spatial * psfs);
   int groups = 1;
   double best = 1e300;
-  LGB_REQUIRE(L >= 1, LGB_EINVAL, "split field: no wavelengths");
   for (int g = std::max(1, std::min(cdiv(L, 16), 16)); g <= std::min(L, 16); ++g) {
     const long long waves = (base * g + cap - 1) / cap;
     const double cost = (double)waves * (double)(cdiv(L, g) + 2);   // waves x work per block
     if (cost < best * (1.0 - 1e-9)) { best = cost; groups = g; }
   }
   groups = cdiv(L, cdiv(L, groups));                 // no empty trailing group
-  LGB_REQUIRE(psfs <= 65535, LGB_EINVAL, "split field: too many PSFs in one launch");
   dim3 grid(cdiv(a.kp, TR) * groups, cdiv(a.n, TC), psfs);
-  if (a.amp) {
-    if (bf16) split_field_T_kernel<true, true><<<grid, 256, 0, s>>>(a, groups);
-    else split_field_T_kernel<false, true><<<grid, 256, 0, s>>>(a, groups);
-  } else {
-    if (bf16) split_field_T_kernel<true, false><<<grid, 256, 0, s>>>(a, groups);
-    else split_field_T_kernel<false, false><<<grid, 256, 0, s>>>(a, groups);
-  }
+  kfn<<<grid, 256, FT_SMEM_BYTES, s>>>(a, groups, map_hi, map_lo);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }

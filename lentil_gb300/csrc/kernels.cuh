@@ -1,6 +1,8 @@
 // Launchers shared between the translation units of the library.
 #pragma once
 
+#include <cuda.h>
+
 #include "common.cuh"
 
 namespace lgb {
@@ -45,6 +47,12 @@ struct SplitFieldArgs {
   int kf_pitch;            // multiple of 8, >= 8 * ceil(kp2 / 256)
 };
 int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s);
+// Tensor map of one plane (hi or lo) of the split f^T operand seen as
+// [Q][n][2][kp] 16-bit values (x = row within a real/imaginary half of K,
+// y = the half, z = field column c, w = problem), box {64, 1, 32, 1} with the
+// 128-byte swizzle: the output tiles of the phasor operand kernel, clipped
+// at kp and n (mft_split.cu).
+int make_field_T_store_map(CUtensorMap* map, const uint16_t* ptr, bool bf16, int kp, int n, int Q);
 
 // max over the slice of |amp| (phasor mode) or max(|re|,|im|) (complex mode)
 int launch_maxabs_amp(const double* amp, int batch, int H, int W, int r0, int c0, int m, int n,

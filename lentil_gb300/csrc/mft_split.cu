@@ -54,6 +54,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <map>
 #include <mutex>
 
@@ -71,7 +72,7 @@ constexpr uint32_t BAR_BYTES = 128;
 constexpr int EPI_WARPS = 8;
 constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
 constexpr uint32_t STG_BYTES = 4096;                       // output staging per epilogue warp
-constexpr unsigned long long WAIT_NS = 2000000000ull;      // 2 s bound on any wait
+constexpr unsigned long long WAIT_NS = 2000000000ull;      // default 2 s bound on any wait
 // K blocks per accumulator drain: 2 for bf16 operands (the fast form: half
 // the drains, and twice the MMA run-ahead across an item's output pass), 1
 // for fp16 (the accurate form: the shortest round-toward-zero chains).
@@ -126,6 +127,11 @@ struct Params {
   const uint8_t* kflags;     // stage 1: field nonzero flags [batch][kf_units][kf_pitch], or null
   int kf_units;              // kp1 / 32 (== kblocks)
   int kf_pitch;
+  unsigned long long wait_ns;  // bound on every mbarrier wait
+  // test of the bounded waits: the producers arrive on the full barrier of
+  // K block stall_kb of item stall_item without issuing its loads, so that
+  // barrier never completes (-1: no such item)
+  int stall_item, stall_kb;
 };
 
 // MMA N of column tile tn: BN, except a narrower last tile when the
@@ -170,20 +176,36 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: true when the phase completed, false on time-out or when
-// another role already flagged an error.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
+// Bounded wait: true when the phase completed, false on time-out (recorded
+// as LGB_ETIMEOUT) or when another role already flagged an error.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err,
+                                          unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = gtimer();
   for (uint32_t n = 1;; ++n) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((n & 63) == 0) {
       if (*(volatile int*)err != 0) return false;
-      if (gtimer() - t0 > WAIT_NS) {
+      if (gtimer() - t0 > limit_ns) {
         atomicCAS(err, 0, LGB_ETIMEOUT);
         return false;
       }
     }
+  }
+}
+// Wait for work this CTA already issued (TMA loads in flight, MMAs) before
+// leaving: bounded in time only, whatever the error flag says, so that a
+// launch that gave up still retires its copies and MMAs before its shared
+// memory and TMEM are released.  Copies and MMAs that were issued complete
+// on their own; only a barrier whose loads were never issued (the stall
+// test) runs out, after limit_ns.
+__device__ __forceinline__ void mbar_wait_issued(uint32_t bar, uint32_t parity,
+                                                 unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return;
+  const uint64_t t0 = gtimer();
+  for (uint32_t n = 1;; ++n) {
+    if (mbar_try_wait(bar, parity)) return;
+    if ((n & 63) == 0 && gtimer() - t0 > limit_ns) return;
   }
 }
 // Shared-memory address of the same variable in CTA `rank` of the cluster.
@@ -341,35 +363,46 @@ struct Live {
   bool all;
 };
 
+// Warp-collective (all 32 lanes, same item): lane l loads the flags of
+// field units l, l+32, l+64, l+96 of the item's column tile at once, the
+// ballots give the unit bitmask, and lane l then decides K blocks l, l+32,
+// ... from it; every lane returns the same set.  One round of loads per
+// item, where a single thread walking the units took up to 128.
 template <int BN>
 __device__ __forceinline__ Live live_kblocks(const Params& p, const Item& w) {
   Live lv{~0ull, ~0ull, p.kblocks, true};
   if (!p.kflags) return lv;
-  uint64_t ulo = 0, uhi = 0;                 // bit u: field unit u is nonzero in the tile
-  const uint8_t* f = p.kflags + (size_t)w.psf * p.kf_units * p.kf_pitch + w.tn * (BN / 32);
-#pragma unroll 8
-  for (int u = 0; u < p.kf_units; ++u) {
-    const uint8_t* fu = f + (size_t)u * p.kf_pitch;
-    const bool nz = BN == 256 ? __ldg(reinterpret_cast<const unsigned long long*>(fu)) != 0ull
-                              : __ldg(reinterpret_cast<const unsigned int*>(fu)) != 0u;
-    if (nz) {
-      if (u < 64) ulo |= 1ull << u;
-      else uhi |= 1ull << (u - 64);
+  const int lane = threadIdx.x & 31;
+  const int U = p.kf_units;
+  const uint8_t* f = p.kflags + (size_t)w.psf * U * p.kf_pitch + w.tn * (BN / 32);
+  uint32_t unit[4];                          // bit l of unit[g]: field unit 32g + l is nonzero
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    const int u = 32 * g + lane;
+    bool nz = false;
+    if (u < U) {
+      const uint8_t* fu = f + (size_t)u * p.kf_pitch;
+      nz = BN == 256 ? __ldg(reinterpret_cast<const unsigned long long*>(fu)) != 0ull
+                     : __ldg(reinterpret_cast<const unsigned int*>(fu)) != 0u;
     }
+    unit[g] = __ballot_sync(0xffffffffu, nz);
   }
-  lv = Live{0ull, 0ull, 0, false};
-  for (int kb = 0; kb < p.kblocks; ++kb) {
-    int u0 = 2 * kb, u1 = 2 * kb + 1;
-    if (u0 >= p.kf_units) u0 -= p.kf_units;
-    if (u1 >= p.kf_units) u1 -= p.kf_units;
-    const uint64_t b0 = u0 < 64 ? ulo >> u0 : uhi >> (u0 - 64);
-    const uint64_t b1 = u1 < 64 ? ulo >> u1 : uhi >> (u1 - 64);
-    if ((b0 | b1) & 1ull) {
-      if (kb < 64) lv.lo |= 1ull << kb;
-      else lv.hi |= 1ull << (kb - 64);
-      ++lv.n;
-    }
+  auto unit_nz = [&](int u) -> uint32_t {      // u < 2U: the imaginary rows wrap onto unit u - U
+    if (u >= U) u -= U;
+    const uint32_t word = u < 32 ? unit[0] : u < 64 ? unit[1] : u < 96 ? unit[2] : unit[3];
+    return (word >> (u & 31)) & 1u;              // (selects, not an indexed load: registers)
+  };
+  uint32_t live[4];
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    const int kb = 32 * g + lane;
+    const bool on = kb < p.kblocks && (unit_nz(2 * kb) | unit_nz(2 * kb + 1));
+    live[g] = __ballot_sync(0xffffffffu, on);
   }
+  lv.lo = live[0] | ((uint64_t)live[1] << 32);
+  lv.hi = live[2] | ((uint64_t)live[3] << 32);
+  lv.n = __popcll(lv.lo) + __popcll(lv.hi);
+  lv.all = false;
   return lv;
 }
 
@@ -552,25 +585,30 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
 
   if (warp == 0) {
     // ------------------------------------------------------ TMA producer
+    // the whole warp walks the items (the live K-block set is a warp
+    // collective); lane 0 issues the copies
     if (lane == 0) {
       prefetch_map(&tmA_hi); prefetch_map(&tmA_lo);
       prefetch_map(&tmB_hi); prefetch_map(&tmB_lo);
-      uint32_t it = 0;
-      bool ok = true;
-      for (int i = pair; ok && i < p.n_items; i += npairs) {
-        const Item w = decode(p, i);
+    }
+    uint32_t it = 0;
+    bool ok = true;
+    for (int i = pair; ok && i < p.n_items; i += npairs) {
+      const Item w = decode(p, i);
+      const Live lv = live_kblocks<BN>(p, w);
+      if (lane == 0) {
         // stage 1: A = E1 block of lam, B = f^T of q; stage 2: A = G of q, B = E2 block of lam
         const int az = p.stage == 1 ? matrix_slot(p, w.lam) : w.q;
         const int bz = p.stage == 1 ? w.q : matrix_slot(p, w.lam);
         const int ay = (2 * w.tm + (int)rank) * BM;
         const int by = w.tn * BN + (int)rank * (tile_n<BN>(p, w.tn) >> 1);
-        const Live lv = live_kblocks<BN>(p, w);
         for (int kb = 0; kb < p.kblocks; ++kb) {
           if (!is_live(lv, kb)) continue;
           const int s = it % STAGES;
-          if (!mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1, p.err)) { ok = false; break; }
+          if (!mbar_wait(empty_bar(s), ((it / STAGES) & 1) ^ 1, p.err, p.wait_ns)) { ok = false; break; }
           const uint32_t fb = map_to_cta(full_bar(s), 0);
           mbar_expect_tx_cluster(fb, STAGE_BYTES);
+          if (i == p.stall_item && kb == p.stall_kb) { ++it; continue; }   // loads withheld
           const uint32_t sa = base + s * STAGE_BYTES;
           tma_load_3d(sa, &tmA_hi, fb, kb * BK, ay, az);
           tma_load_3d(sa + A_BYTES, &tmA_lo, fb, kb * BK, ay, az);
@@ -579,56 +617,65 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
           ++it;
         }
       }
-      // every copy of both CTAs has landed before the pair exits (the even
-      // CTA's full barriers count the odd CTA's bytes too)
-      if (leader)
-        for (uint32_t k = (it > STAGES ? it - STAGES : 0); k < it; ++k)
-          mbar_wait(full_bar(k % STAGES), (k / STAGES) & 1, p.err);
+      ok = __shfl_sync(0xffffffffu, ok, 0) != 0;
     }
+    // every copy of both CTAs has landed before the pair exits (the even
+    // CTA's full barriers count the odd CTA's bytes too)
+    if (lane == 0 && leader)
+      for (uint32_t k = (it > STAGES ? it - STAGES : 0); k < it; ++k)
+        mbar_wait_issued(full_bar(k % STAGES), (k / STAGES) & 1, p.wait_ns);
   } else if (warp == 1) {
     // ------------------------------------------------------- MMA issuer
-    if (leader && lane == 0) {
+    // (even CTA) the whole warp walks the items (the live K-block set is a
+    // warp collective); lane 0 issues the MMAs and the commits
+    if (leader) {
       uint32_t it = 0;                       // K blocks issued (stage ring)
       uint32_t gi = 0;                       // accumulator groups issued (accumulator uses)
       bool ok = true;
       for (int i = pair; ok && i < p.n_items; i += npairs) {
         const Item w = decode(p, i);
-        const uint32_t idesc = (p.idesc & ~(0x3Fu << 17)) |
-                               ((uint32_t)(tile_n<BN>(p, w.tn) >> 3) << 17);
         const Live lv = live_kblocks<BN>(p, w);
-        int j = 0;                           // live K blocks of this item issued
-        for (int kb = 0; kb < p.kblocks; ++kb) {
-          if (!is_live(lv, kb)) continue;
-          const int s = it % STAGES, xb = gi & 1;
-          const bool first = j % Drain<BF16>::KB == 0;
-          const bool last = j % Drain<BF16>::KB == Drain<BF16>::KB - 1 || j == lv.n - 1;
-          if (!mbar_wait(full_bar(s), (it / STAGES) & 1, p.err)) { ok = false; break; }
-          // accumulator xb was drained by both CTAs (its previous group, gi - 2)
-          if (first && !mbar_wait(acc_empty(xb), ((gi >> 1) & 1) ^ 1, p.err)) { ok = false; break; }
-          tc_fence_after();
-          const uint32_t sa = base + s * STAGE_BYTES, X = tmem + xb * ACC_COLS;
+        if (lane == 0) {
+          const uint32_t idesc = (p.idesc & ~(0x3Fu << 17)) |
+                                 ((uint32_t)(tile_n<BN>(p, w.tn) >> 3) << 17);
+          int j = 0;                         // live K blocks of this item issued
+          for (int kb = 0; kb < p.kblocks; ++kb) {
+            if (!is_live(lv, kb)) continue;
+            const int s = it % STAGES, xb = gi & 1;
+            const bool first = j % Drain<BF16>::KB == 0;
+            const bool last = j % Drain<BF16>::KB == Drain<BF16>::KB - 1 || j == lv.n - 1;
+            if (!mbar_wait(full_bar(s), (it / STAGES) & 1, p.err, p.wait_ns)) { ok = false; break; }
+            // accumulator xb was drained by both CTAs (its previous group, gi - 2)
+            if (first && !mbar_wait(acc_empty(xb), ((gi >> 1) & 1) ^ 1, p.err, p.wait_ns)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t sa = base + s * STAGE_BYTES, X = tmem + xb * ACC_COLS;
 #pragma unroll
-          for (int k = 0; k < KSTEPS; ++k) {     // hi.lo + lo.hi: small terms first
-            mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + B_BYTES + k * 32),
-                    idesc, (first && k == 0) ? 0u : 1u);
-            mma_f16(X, smem_desc(sa + A_BYTES + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32),
-                    idesc, 1u);
-          }
+            for (int k = 0; k < KSTEPS; ++k) {   // hi.lo + lo.hi: small terms first
+              mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + B_BYTES + k * 32),
+                      idesc, (first && k == 0) ? 0u : 1u);
+              mma_f16(X, smem_desc(sa + A_BYTES + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32),
+                      idesc, 1u);
+            }
 #pragma unroll
-          for (int k = 0; k < KSTEPS; ++k)       // hi.hi last
-            mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32), idesc, 1u);
-          mma_commit_pair(empty_bar(s));         // both CTAs' stage s free once these retire
-          if (last) {
-            mma_commit_pair(acc_full(xb));       // accumulator xb ready for the epilogues
-            ++gi;
+            for (int k = 0; k < KSTEPS; ++k)     // hi.hi last
+              mma_f16(X, smem_desc(sa + k * 32), smem_desc(sa + 2 * A_BYTES + k * 32), idesc, 1u);
+            mma_commit_pair(empty_bar(s));       // both CTAs' stage s free once these retire
+            if (last) {
+              mma_commit_pair(acc_full(xb));     // accumulator xb ready for the epilogues
+              ++gi;
+            }
+            ++j;
+            ++it;
           }
-          ++j;
-          ++it;
         }
+        ok = __shfl_sync(0xffffffffu, ok, 0) != 0;
       }
       // all issued MMAs have retired before TMEM is released
-      mma_commit_pair(drain_bar);
-      mbar_wait(drain_bar, 0, p.err);
+      if (lane == 0) {
+        mma_commit_pair(drain_bar);
+        mbar_wait_issued(drain_bar, 0, p.wait_ns);
+      }
+      __syncwarp();
     }
   } else {
     // --------------------------------------------------------- epilogue
@@ -651,7 +698,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
       for (int j = 0; j < C::RUN; ++j) run[j] = 0.f;
       for (int g = 0; g < groups; ++g, ++gi) {
         const int xb = gi & 1;
-        ok = __all_sync(0xffffffffu, mbar_wait(acc_full(xb), (gi >> 1) & 1, p.err));
+        ok = __all_sync(0xffffffffu, mbar_wait(acc_full(xb), (gi >> 1) & 1, p.err, p.wait_ns));
         if (!ok) break;
         tc_fence_after();
         drain_add<C::RUN>(trow + xb * ACC_COLS, p.stage, ch, run);
@@ -722,6 +769,27 @@ static int make_map(CUtensorMap* map, const void* ptr, bool bf16, int K, int row
   return make_map_any(map, ptr, half_type(bf16), 2, K, rows, batch, BK, box_rows,
                       CU_TENSOR_MAP_SWIZZLE_128B);
 }
+
+}  // namespace tc
+
+int make_field_T_store_map(CUtensorMap* map, const uint16_t* ptr, bool bf16, int kp, int n, int Q) {
+  auto enc = tc::encode_fn();
+  LGB_REQUIRE(enc, LGB_ECUDA, "cuTensorMapEncodeTiled is unavailable");
+  LGB_REQUIRE(((uintptr_t)ptr & 15) == 0, LGB_EINVAL, "tensor map base must be 16-byte aligned");
+  LGB_REQUIRE(kp % 32 == 0 && n > 0 && Q > 0, LGB_EINVAL, "split field map: bad shape");
+  cuuint64_t dims[4] = {(cuuint64_t)kp, 2, (cuuint64_t)n, (cuuint64_t)Q};
+  cuuint64_t strides[3] = {(cuuint64_t)kp * 2, (cuuint64_t)kp * 4, (cuuint64_t)kp * 4 * n};
+  cuuint32_t box[4] = {64, 1, 32, 1};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult res = enc(map, tc::half_type(bf16), 4, const_cast<uint16_t*>(ptr), dims, strides, box,
+                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (res != CUDA_SUCCESS)
+    return set_error(LGB_ECUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)res));
+  return LGB_OK;
+}
+
+namespace tc {
 
 constexpr uint32_t make_idesc(bool bf16, int bn) {
   return (1u << 4)                          // D format: FP32
@@ -811,6 +879,13 @@ static void stage_shapes(const SplitMftProblem& q, int bn, StageShape (&st)[2]) 
   st[1].kblocks = 2 * q.kp2 / BK;
 }
 
+// One-shot test of the bounded waits (lgb_test_stall_tma): the next stage-1
+// launch withholds the loads of one K block and bounds its waits by
+// g_stall_wait nanoseconds.
+static std::atomic<int> g_stall_item{-1};
+static std::atomic<int> g_stall_kb{0};
+static std::atomic<unsigned long long> g_stall_wait{WAIT_NS};
+
 // Both stages with pair tiles BN wide; ev (optional [4]) brackets the two
 // launches.  Every tensor map is encoded before the first launch, so the
 // host leaves no gap between the stages on the stream.
@@ -852,6 +927,12 @@ static int run_split_mft(const SplitMftProblem& q, cudaEvent_t* ev, cudaStream_t
 
   Params p{};
   p.stage = 1;
+  p.wait_ns = WAIT_NS;
+  p.stall_item = g_stall_item.exchange(-1);
+  if (p.stall_item >= 0) {
+    p.stall_kb = g_stall_kb.load();
+    p.wait_ns = g_stall_wait.load();
+  }
   p.kblocks = sh[0].kblocks;
   p.m_tiles = cdiv(cdiv(q.M, 64), 2);          // pairs of 64-row (128 block-row) E1 tiles
   p.n_tiles = cdiv(q.kp2, BN);
@@ -878,6 +959,8 @@ static int run_split_mft(const SplitMftProblem& q, cudaEvent_t* ev, cudaStream_t
   if (ev) LGB_CUDA(cudaEventRecord(ev[1], s));
 
   p.stage = 2;
+  p.stall_item = -1;
+  p.wait_ns = WAIT_NS;
   p.kflags = nullptr;                           // G is dense
   p.kblocks = sh[1].kblocks;
   p.m_tiles = cdiv(q.M, 2 * BM);
@@ -1101,6 +1184,16 @@ int launch_split_mft(const SplitMftProblem& q, cudaStream_t s) {
 
 // ------------------------------------------------------------- tuner ABI ---
 using namespace lgb;
+
+extern "C" int lgb_test_stall_tma(int item, int kblock, double wait_ms) {
+  LGB_REQUIRE(item >= 0 && kblock >= 0, LGB_EINVAL, "test_stall_tma: item and kblock must be >= 0");
+  LGB_REQUIRE(wait_ms > 0.0 && wait_ms <= 2000.0, LGB_EINVAL,
+              "test_stall_tma: wait_ms must lie in (0, 2000]");
+  tc::g_stall_kb.store(kblock);
+  tc::g_stall_wait.store((unsigned long long)(wait_ms * 1e6));
+  tc::g_stall_item.store(item);
+  return LGB_OK;
+}
 
 extern "C" int lgb_tuner_set_mode(int mode) {
   LGB_REQUIRE(mode == LGB_TUNE_MODEL || mode == LGB_TUNE_MEASURE, LGB_EINVAL,

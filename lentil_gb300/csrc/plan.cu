@@ -272,7 +272,8 @@ struct lgb_psf_plan_s {
   std::vector<double> lam, ar, ac, sr, sc;
   void* mem = nullptr;
   size_t bytes = 0;
-  cudaStream_t stream = nullptr;   // creation stream: the plan's memory is freed on it
+  bool owns_mem = true;            // false: caller memory (lgb_psf_plan_create_in)
+  cudaStream_t stream = nullptr;   // creation stream: the plan's own memory is freed on it
   int kp1 = 0, kp2 = 0;
   // device views
   int* err = nullptr;
@@ -347,11 +348,7 @@ static int prof_end(lgb_psf_plan_s* P, int slot, cudaStream_t s, cudaEvent_t* e)
   return LGB_OK;
 }
 
-extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan, lgb_stream stream) {
-  LGB_RANGE("lgb_psf_plan_create");
-  LGB_REQUIRE(desc && plan, LGB_EINVAL, "psf_plan_create: null argument");
-  const lgb_psf_desc& d = *desc;
-  *plan = nullptr;
+static int check_desc(const lgb_psf_desc& d) {
   LGB_REQUIRE(d.H > 0 && d.W > 0 && d.m > 0 && d.n > 0 && d.M > 0 && d.N > 0, LGB_EINVAL,
               "psf_plan_create: sizes must be positive");
   LGB_REQUIRE(d.r0 >= 0 && d.c0 >= 0 && d.r0 + d.m <= d.H && d.c0 + d.n <= d.W, LGB_EINVAL,
@@ -367,6 +364,11 @@ extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan,
               LGB_EINVAL, "psf_plan_create: batch must be positive (0: split matrices only)");
   LGB_REQUIRE(d.precision == LGB_FP64 || is_split(d.precision), LGB_EINVAL,
               "psf_plan_create: unknown precision");
+  return LGB_OK;
+}
+
+// A plan object for desc with its tables copied (no device memory yet).
+static lgb_psf_plan_s* new_plan(const lgb_psf_desc& d) {
   const int L = d.n_wavelengths;
   auto P = new lgb_psf_plan_s();
   P->d = d;
@@ -379,13 +381,20 @@ extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan,
   P->kp1 = round_up(d.m, 32);
   P->kp2 = round_up(d.n, 32);
   P->bytes = plan_carve(P, nullptr);
-  cudaStream_t s = as_stream(stream);
-  P->stream = s;
-  cudaError_t e = cudaMallocAsync(&P->mem, P->bytes, s);
-  if (e != cudaSuccess) {
-    delete P;
-    return check_cuda(e, "cudaMallocAsync(psf plan)");
-  }
+  return P;
+}
+
+static void free_plan(lgb_psf_plan_s* P, cudaStream_t s) {
+  if (P->owns_mem && P->mem) cudaFreeAsync(P->mem, s);
+  delete P;
+}
+
+// Fill a plan whose memory is in place: tables to the device, then the DFT
+// matrices of every wavelength (resident for the plan's lifetime).
+static int build_plan(lgb_psf_plan_s* P, cudaStream_t s, lgb_psf_plan* plan) {
+  const lgb_psf_desc& d = P->d;
+  const int L = d.n_wavelengths;
+  cudaError_t e = cudaSuccess;
   plan_carve(P, P->mem);
 
   // host tables -> device
@@ -401,10 +410,9 @@ extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan,
     const float hi = (float)tol[l];
     kh[l] = make_float2(hi, (float)(tol[l] - (double)hi));
   }
-  if (st) { cudaFreeAsync(P->mem, s); delete P; return st; }
+  if (st) { free_plan(P, s); return st; }
   auto fail = [&](cudaError_t err, const char* what) {
-    cudaFreeAsync(P->mem, s);
-    delete P;
+    free_plan(P, s);
     return check_cuda(err, what);
   };
   if ((e = cudaMemcpyAsync(P->axes, axes.data(), sizeof(PhaseAxis) * axes.size(), cudaMemcpyHostToDevice, s))) return fail(e, "copy axes");
@@ -425,9 +433,54 @@ extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan,
       if (!st) st = launch_dft_matrix_c128(axes[L + l], d.n, d.N, P->E2 + (size_t)l * d.n * d.N, false, s);
     }
   }
-  if (st) { cudaFreeAsync(P->mem, s); delete P; return st; }
+  if (st) { free_plan(P, s); return st; }
   *plan = P;
   return LGB_OK;
+}
+
+extern "C" int lgb_psf_plan_create(const lgb_psf_desc* desc, lgb_psf_plan* plan, lgb_stream stream) {
+  LGB_RANGE("lgb_psf_plan_create");
+  LGB_REQUIRE(desc && plan, LGB_EINVAL, "psf_plan_create: null argument");
+  *plan = nullptr;
+  int st = check_desc(*desc);
+  if (st) return st;
+  lgb_psf_plan_s* P = new_plan(*desc);
+  cudaStream_t s = as_stream(stream);
+  P->stream = s;
+  cudaError_t e = cudaMallocAsync(&P->mem, P->bytes, s);
+  if (e != cudaSuccess) {
+    delete P;
+    return check_cuda(e, "cudaMallocAsync(psf plan)");
+  }
+  return build_plan(P, s, plan);
+}
+
+extern "C" size_t lgb_psf_plan_size(const lgb_psf_desc* desc) {
+  if (!desc || check_desc(*desc) != LGB_OK) return 0;
+  lgb_psf_plan_s* P = new_plan(*desc);
+  const size_t bytes = P->bytes;
+  delete P;
+  return bytes;
+}
+
+extern "C" int lgb_psf_plan_create_in(const lgb_psf_desc* desc, void* memory, size_t memory_bytes,
+                                      lgb_psf_plan* plan, lgb_stream stream) {
+  LGB_RANGE("lgb_psf_plan_create_in");
+  LGB_REQUIRE(desc && plan, LGB_EINVAL, "psf_plan_create_in: null argument");
+  *plan = nullptr;
+  int st = check_desc(*desc);
+  if (st) return st;
+  LGB_REQUIRE(memory && ((uintptr_t)memory & 255) == 0, LGB_EWORKSPACE,
+              "psf_plan_create_in: memory must be non-null and 256-byte aligned");
+  lgb_psf_plan_s* P = new_plan(*desc);
+  if (memory_bytes < P->bytes) {
+    delete P;
+    return set_error(LGB_EWORKSPACE, "psf_plan_create_in: memory smaller than lgb_psf_plan_size");
+  }
+  P->mem = memory;
+  P->owns_mem = false;
+  P->stream = as_stream(stream);
+  return build_plan(P, P->stream, plan);
 }
 
 extern "C" size_t lgb_psf_plan_bytes(lgb_psf_plan plan) { return plan ? plan->bytes : 0; }
@@ -621,9 +674,10 @@ extern "C" int lgb_psf_plan_status(lgb_psf_plan P, lgb_stream stream) {
 
 extern "C" int lgb_psf_plan_destroy(lgb_psf_plan P) {
   if (!P) return LGB_OK;
-  // stream-ordered free: no device-wide synchronisation; the caller destroys
-  // a plan only after the work that used it has completed
-  cudaError_t e = cudaFreeAsync(P->mem, P->stream);
+  // stream-ordered free of the plan's own memory: no device-wide
+  // synchronisation; the caller destroys a plan only after the work that
+  // used it has completed (caller memory is left to the caller)
+  cudaError_t e = P->owns_mem ? cudaFreeAsync(P->mem, P->stream) : cudaSuccess;
   delete P;
   if (e != cudaSuccess) return check_cuda(e, "cudaFree(psf plan)");
   return LGB_OK;

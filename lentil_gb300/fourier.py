@@ -42,6 +42,8 @@ class _Dft2Plan:
         _lib.call('lgb_dft2_plan_create_in', m, n, M, N, ar, ac, sr, sc, orow, ocol, unitary, prec,
                   self._mem.data_ptr(), self.nbytes, dv.stream_ptr(), ctypes.byref(h))
         self._h = h
+        self._built = torch.cuda.Event()      # the matrix build, on the creating stream
+        self._built.record(self._home)
         self.shape_out = (M, N)
         self.split = prec != _lib.FP64
         self.pins = 0                 # > 0 while a captured CUDA graph holds its pointers
@@ -51,10 +53,11 @@ class _Dft2Plan:
         A device-side failure of an earlier execute is raised here."""
         count = int(fd.shape[0])
         s = torch.cuda.current_stream()
-        if s != self._home and s.cuda_stream not in self._foreign and \
-                not torch.cuda.is_current_stream_capturing():
-            self._mem.record_stream(s)        # keep the matrices until s is done with them
-            self._foreign.add(s.cuda_stream)
+        if s != self._home and not torch.cuda.is_current_stream_capturing():
+            s.wait_event(self._built)         # the matrices are built before s reads them
+            if s.cuda_stream not in self._foreign:
+                self._mem.record_stream(s)    # keep the matrices until s is done with them
+                self._foreign.add(s.cuda_stream)
         F = torch.empty((count,) + self.shape_out, dtype=torch.complex128, device=fd.device)
         nbytes = self._lib.lgb_dft2_plan_workspace_size(self._h, count)
         ws = dv.workspace(nbytes)
