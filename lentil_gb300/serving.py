@@ -26,11 +26,18 @@ weights, optics) are queued by any thread and scheduled by one GPU thread:
   CUDA graph (one per tile width; for the tuned width only once the tuner has
   decided the launch class) that later launches replay;
 - completion is detected with CUDA events; latency is submit -> result;
+- pupils and OPD bases can be made device-resident once
+  (``PSFServer.resident_pupil`` / ``resident_basis``): a request that names
+  a resident pupil and gives its OPD as modal coefficients of a resident
+  basis sends only its coefficients to the device (the OPD map is expanded
+  there by ``lgb_basis_expand``), and its geometry key needs no scan of the
+  amplitude; requests with plain arrays are staged through pinned memory;
 - a request whose plan cannot be built, or a launch whose buffers cannot be
   allocated, fails with that exception while the server keeps serving; any
   other error of the scheduling loop fails the queued requests instead of
   leaving their futures waiting.
 """
+import itertools
 import collections
 import concurrent.futures
 import threading
@@ -47,13 +54,47 @@ from .broadband import make_plan, plan_geometry
 from .ptype import pupil as PUPIL
 
 
+_resident_ids = itertools.count(1)
+
+
+class Resident:
+    """A pupil-plane array held on the device for the life of the object:
+    a pupil amplitude (float64 [H, W], mask applied, with its boundary slice
+    computed once) or an OPD basis (float32 [K, H, W]).  Made by
+    ``PSFServer.resident_pupil`` / ``resident_basis``; requests refer to it
+    instead of carrying the array."""
+
+    def __init__(self, array, dtype, device, slice_=None):
+        self.tensor = torch.as_tensor(np.ascontiguousarray(array), dtype=dtype).to(device)
+        torch.cuda.current_stream(device).synchronize()   # on the device before any launch reads it
+        self.shape = tuple(self.tensor.shape)
+        self.key = next(_resident_ids)
+        self.slice = slice_
+
+
 class PSFRequest:
-    """One broadband PSF: sum_lambda w * |propagate_dft(Wavefront(lambda) * pupil)|^2."""
+    """One broadband PSF: sum_lambda w * |propagate_dft(Wavefront(lambda) * pupil)|^2.
+
+    ``amp``: amplitude array (mask applied) or a resident pupil.  ``opd``:
+    OPD map (metres), or, with ``opd_basis`` (a resident basis of K modes),
+    the K modal coefficients of the OPD."""
 
     def __init__(self, amp, opd, wavelengths, weights, pixelscale_in, focal_length,
-                 det_pixelscale, det_shape, oversample=2):
-        self.amp = np.ascontiguousarray(amp, dtype=np.float64)   # mask applied
-        self.opd = np.ascontiguousarray(opd, dtype=np.float64)
+                 det_pixelscale, det_shape, oversample=2, opd_basis=None):
+        self.amp = amp if isinstance(amp, Resident) else np.ascontiguousarray(amp, dtype=np.float64)
+        self.opd_basis = opd_basis
+        if opd_basis is not None:
+            if not isinstance(opd_basis, Resident) or len(opd_basis.shape) != 3:
+                raise TypeError('opd_basis must be a resident basis (PSFServer.resident_basis)')
+            self.opd = np.ascontiguousarray(opd, dtype=np.float64).reshape(-1)
+            if self.opd.size != opd_basis.shape[0]:
+                raise ValueError('one OPD coefficient per basis mode')
+            if opd_basis.shape[1:] != self.plane_shape:
+                raise ValueError('OPD basis and pupil shapes differ')
+        else:
+            self.opd = np.ascontiguousarray(opd, dtype=np.float64)
+            if self.opd.shape != self.plane_shape:
+                raise ValueError('OPD and pupil shapes differ')
         self.wavelengths = np.atleast_1d(np.asarray(wavelengths, dtype=np.float64))
         self.weights = np.atleast_1d(np.asarray(weights, dtype=np.float64))
         if self.weights.shape != self.wavelengths.shape:
@@ -64,13 +105,22 @@ class PSFRequest:
         self.det_shape = int(det_shape)
         self.oversample = int(oversample)
         self.future = concurrent.futures.Future()
-        self.t_submit = self.t_done = None
+        self.t_submit = self.t_launch = self.t_done = None
         self._geo_key = None
+
+    @property
+    def plane_shape(self):
+        return tuple(self.amp.shape)
+
+    def field_slice(self):
+        if isinstance(self.amp, Resident):
+            return self.amp.slice
+        return util.boundary_slice(self.amp)
 
     def geometry_key(self):
         if self._geo_key is None:
-            s = util.boundary_slice(self.amp)
-            self._geo_key = (self.amp.shape, self.pixelscale_in, self.focal_length,
+            s = self.field_slice()
+            self._geo_key = (self.plane_shape, self.pixelscale_in, self.focal_length,
                              self.det_pixelscale, self.det_shape, self.oversample,
                              (s[0].start, s[0].stop, s[1].start, s[1].stop))
         return self._geo_key
@@ -78,6 +128,11 @@ class PSFRequest:
     @property
     def latency(self):
         return None if self.t_done is None else self.t_done - self.t_submit
+
+    @property
+    def queue_wait(self):
+        """Seconds from submission to the launch that computed the request."""
+        return None if self.t_launch is None else self.t_launch - self.t_submit
 
 
 def plan_bytes_estimate(plane_shape, fslice, window, L, batch, precision):
@@ -98,27 +153,78 @@ class _Buffers:
     """Device and pinned host buffers of one launch shape (n PSFs, n_sel
     wavelengths), optionally with the launch captured as a CUDA graph."""
 
+    KMAX = 1024                   # modal coefficients per PSF (lgb_basis_expand's limit)
+
     def __init__(self, slot, n, n_sel, device):
         H, W = slot.geo.plane_shape
         self.n, self.n_sel = n, n_sel
+        self.shape_out = (n,) + slot.geo.shape_out
         self.A = torch.empty((n, H, W), dtype=torch.float64, device=device)
         self.O = torch.empty_like(self.A)
         self.Wt = torch.empty(n * n_sel, dtype=torch.float64, device=device)
         self.lam = torch.empty(n_sel, dtype=torch.int32, device=device)
-        self.out = torch.empty((n,) + slot.geo.shape_out, dtype=torch.float64, device=device)
+        self.C = torch.empty((n, self.KMAX), dtype=torch.float64, device=device)
+        self.out = torch.empty(self.shape_out, dtype=torch.float64, device=device)
         self.ws = torch.empty(max(1, slot.plan.workspace_bytes(n, n_sel)), dtype=torch.uint8,
                               device=device)
-        self.hA = torch.empty((n, H, W), dtype=torch.float64, pin_memory=True)
-        self.hO = torch.empty_like(self.hA, pin_memory=True)
+        self.hA = self.hO = None      # pinned staging of plain arrays, made when first needed
         self.hW = torch.empty(n * n_sel, dtype=torch.float64, pin_memory=True)
         self.hlam = torch.empty(n_sel, dtype=torch.int32, pin_memory=True)
-        self.hout = torch.empty((n,) + slot.geo.shape_out, dtype=torch.float64, pin_memory=True)
+        self.hC = torch.empty((n, self.KMAX), dtype=torch.float64, pin_memory=True)
+        self.hout = None              # this launch's results (pinned, handed to the requests)
+        self.reqs = []
         self.graphs = {}              # tile width -> captured launch
         self.busy = False
 
+    def stage(self, slot, batch):
+        """Host side of a launch: plain arrays into pinned staging, modal
+        coefficients, weights and the wavelength subset."""
+        self.reqs = batch
+        hW = self.hW.view(len(batch), self.n_sel).numpy()
+        hC = self.hC.numpy()
+        for k, r in enumerate(batch):
+            if not isinstance(r.amp, Resident):
+                if self.hA is None:
+                    self.hA = torch.empty(tuple(self.A.shape), dtype=torch.float64, pin_memory=True)
+                self.hA[k].numpy()[...] = r.amp
+            if r.opd_basis is not None:
+                hC[k, :r.opd.size] = r.opd
+            else:
+                if self.hO is None:
+                    self.hO = torch.empty(tuple(self.O.shape), dtype=torch.float64, pin_memory=True)
+                self.hO[k].numpy()[...] = r.opd
+            hW[k] = r.weights if slot.grid else r.weights[slot.geo.keep]
+        if slot.grid:
+            self.hlam.numpy()[...] = batch[0]._subset
+        # results land in a block of torch's caching host allocator that the
+        # requests keep (no copy on the scheduling thread)
+        self.hout = torch.empty(self.shape_out, dtype=torch.float64, pin_memory=True)
+
+    def load(self, slot, stream):
+        """Device side of the inputs, on ``stream``: resident pupils copied
+        on the device, plain arrays from pinned staging, modal OPDs expanded
+        from their coefficients."""
+        P = self.A.shape[1] * self.A.shape[2]
+        if any(r.opd_basis is not None for r in self.reqs):
+            self.C.copy_(self.hC, non_blocking=True)
+        for k, r in enumerate(self.reqs):
+            if isinstance(r.amp, Resident):
+                self.A[k].copy_(r.amp.tensor, non_blocking=True)
+            else:
+                self.A[k].copy_(self.hA[k], non_blocking=True)
+            if r.opd_basis is not None:
+                _lib.call('lgb_basis_expand', r.opd_basis.tensor.data_ptr(), self.C[k].data_ptr(),
+                          int(r.opd.size), P, self.O[k].data_ptr(), stream.cuda_stream)
+            else:
+                self.O[k].copy_(self.hO[k], non_blocking=True)
+        self.Wt.copy_(self.hW, non_blocking=True)
+        if slot.grid:
+            self.lam.copy_(self.hlam, non_blocking=True)
+
     @property
     def nbytes(self):
-        return 8 * (2 * self.A.numel() + self.Wt.numel() + self.out.numel()) + self.ws.numel()
+        return 8 * (2 * self.A.numel() + self.Wt.numel() + self.C.numel() + self.out.numel()) + \
+            self.ws.numel()
 
     def launch(self, slot):
         lam = self.lam if slot.grid else None
@@ -166,14 +272,9 @@ class _Slot:
     def run(self, b, stream, reuse, tile):
         """Launch buffers ``b`` (host inputs already staged) on ``stream``
         with pair-tile width ``tile`` (0: the autotuner's)."""
-        n, n_sel = b.n, b.n_sel
         self.plan.set_tile(tile)
         with torch.cuda.stream(stream):
-            b.A.copy_(b.hA, non_blocking=True)
-            b.O.copy_(b.hO, non_blocking=True)
-            b.Wt.copy_(b.hW, non_blocking=True)
-            if self.grid:
-                b.lam.copy_(b.hlam, non_blocking=True)
+            b.load(self, stream)
             g = b.graphs.get(tile)
             if reuse and g is None and (tile != 0 or self.tile_decided(b)):
                 b.launch(self)                       # warm-up outside capture
@@ -226,10 +327,27 @@ class PSFServer:
         self._streams = []
         self._stop = False
         self.stats = collections.Counter()
+        # (perf_counter time, kind, value): 'build' (plan build seconds on the
+        # scheduler thread), 'evict' (plan bytes released)
+        self.events = []
         self._thread = threading.Thread(target=self._loop, name='psf-server', daemon=True)
         self._thread.start()
 
     # ------------------------------------------------------------ public
+    def resident_pupil(self, amp):
+        """Keep a pupil amplitude (mask applied) on the device; requests
+        that name it copy it on the device instead of sending it."""
+        a = np.ascontiguousarray(amp, dtype=np.float64)
+        return Resident(a, torch.float64, self.device, util.boundary_slice(a))
+
+    def resident_basis(self, modes):
+        """Keep an OPD basis ([K, H, W], K <= 1024) on the device as FP32;
+        requests give their OPD as K coefficients of it."""
+        m = np.asarray(modes)
+        if m.ndim != 3 or not 1 <= m.shape[0] <= _Buffers.KMAX:
+            raise ValueError('an OPD basis is [K, H, W] with 1 <= K <= 1024')
+        return Resident(m, torch.float32, self.device)
+
     def submit(self, req):
         if req.future.done():                      # a request object may be submitted again
             req.future = concurrent.futures.Future()
@@ -334,9 +452,10 @@ class PSFServer:
                 if r.future.done():
                     continue
                 if err is None:
-                    r.future.set_result(b.hout[k].numpy().copy())
+                    r.future.set_result(b.hout[k].numpy())
                 else:
                     r.future.set_exception(err)
+            b.hout = None
             b.busy = False
             slot.inflight -= 1
             self._free_streams.append(si)
@@ -351,6 +470,7 @@ class PSFServer:
             if slot.inflight == 0:
                 del self._slots[key]
                 self._bytes -= slot.bytes
+                self.events.append((time.perf_counter(), 'evict', slot.bytes))
                 del slot
                 self.stats['evicted'] += 1
         return self._bytes + need <= self.budget
@@ -364,8 +484,8 @@ class PSFServer:
             return slot
         grid = req._subset is not None
         wl = self.grid if grid else req.wavelengths
-        s = util.boundary_slice(req.amp)
-        geo = plan_geometry(req.amp.shape, s, [], np.broadcast_to(req.pixelscale_in, (2,)),
+        s = req.field_slice()
+        geo = plan_geometry(req.plane_shape, s, [], np.broadcast_to(req.pixelscale_in, (2,)),
                             req.focal_length, PUPIL, wl, req.det_pixelscale,
                             shape=req.det_shape, oversample=req.oversample)
         if geo.window_shape is None or (grid and len(geo.keep) != len(wl)):
@@ -377,7 +497,9 @@ class PSFServer:
             return 'too_big'
         if not self._make_room(int(est * 1.05)):
             return None                               # wait for running work to finish
+        t0 = time.perf_counter()
         slot = _Slot(key, geo, self.precision, grid)
+        self.events.append((t0, 'build', time.perf_counter() - t0))
         self._slots[key] = slot
         self._bytes += slot.bytes
         self.stats['plans_built'] += 1
@@ -435,14 +557,11 @@ class PSFServer:
                     self._alloc_failures -= 1
                     raise torch.cuda.OutOfMemoryError('injected allocation failure')
                 b, reuse = slot.buffers(len(batch), n_sel, self.device, self.use_graphs)
-                hW = b.hW.view(len(batch), n_sel).numpy()
-                for k, r in enumerate(batch):
-                    b.hA[k].numpy()[...] = r.amp
-                    b.hO[k].numpy()[...] = r.opd
-                    hW[k] = r.weights if slot.grid else r.weights[slot.geo.keep]
-                if slot.grid:
-                    b.hlam.numpy()[...] = batch[0]._subset
+                b.stage(slot, batch)
                 b.busy = True
+                t_launch = time.perf_counter()
+                for r in batch:
+                    r.t_launch = t_launch
                 tile = self.SHARED_TILE if self._inflight else 0
                 ev = slot.run(b, self._streams[si], reuse, tile)
             except (MemoryError, RuntimeError) as e:     # torch OOM is a RuntimeError

@@ -145,3 +145,34 @@ def test_server_tuner_cache_file(cuda_device, tmp_path):
     tuner.clear()
     with serving.PSFServer(streams=1, max_batch=1, precision='split', tuner_cache=str(path)):
         assert tuner.entries() == decided
+
+
+def test_resident_pupil_and_modal_opd(cuda_device):
+    # requests naming a device-resident pupil and giving their OPD as
+    # coefficients of a resident Zernike basis (expanded on the GPU) equal
+    # the same requests carrying the arrays, and the oracle
+    rng = np.random.default_rng(11)
+    npix = 96
+    amp = lg.normalize_power(lg.circle((npix, npix), npix * 0.45))
+    support = amp > 0
+    rho, th = lg.zernike_coordinates(support)
+    basis = np.asarray([lg.zernike(support, j, rho=rho, theta=th) for j in range(2, 12)])
+    basis32 = basis.astype(np.float32)
+    with serving.PSFServer(streams=2, max_batch=2, precision='split') as srv:
+        pup, bas = srv.resident_pupil(amp), srv.resident_basis(basis32)
+        modal, raw = [], []
+        for L in (3, 5, 3, 1):
+            c = rng.normal(0, 30e-9, 10)
+            wl = np.linspace(450e-9, 900e-9, L) if L > 1 else np.array([650e-9])
+            w = np.full(L, 1.0 / L)
+            args = (wl, w, 1.0 / npix, 10.0, 5e-6 * 256 / npix, 24)
+            modal.append(serving.PSFRequest(pup, c, *args, opd_basis=bas))
+            raw.append(serving.PSFRequest(amp, np.tensordot(c, basis32.astype(np.float64), 1), *args))
+        out_m = [f.result(timeout=120) for f in [srv.submit(r) for r in modal]]
+        out_r = [f.result(timeout=120) for f in [srv.submit(r) for r in raw]]
+    for r, a, b in zip(raw, out_m, out_r):
+        assert lo.peak_normalised_error(a, b) < TOL
+        assert lo.peak_normalised_error(a, _alone(r)) < TOL
+    with pytest.raises(ValueError):
+        serving.PSFRequest(pup, np.zeros(3), np.array([6e-7]), np.ones(1), 1.0 / npix, 10.0, 5e-6,
+                           24, opd_basis=bas)
