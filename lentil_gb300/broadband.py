@@ -243,14 +243,35 @@ def dense_field(pupil):
     if amp.ndim != 2:
         raise NotImplementedError('broadband plan needs an amplitude array')
     gmask = mask if mask.ndim == 2 else mask.sum(axis=0)
-    if mask.ndim == 2:
-        s = util.boundary_slice(mask)
-    else:
-        sl = [util.boundary_slice(x) for x in mask]
-        s = np.s_[min(x[0].start for x in sl):max(x[0].stop for x in sl),
-                  min(x[1].start for x in sl):max(x[1].stop for x in sl)]
+    # the union of the segments' bounding boxes: segment masks are
+    # transmissions (>= 0), so a pixel lies in some segment exactly where
+    # their sum is positive -- one scan of the summed mask instead of one
+    # per segment
+    s = util.boundary_slice(gmask)
     opd_full = np.broadcast_to(opd, amp.shape) if opd.size == 1 else opd
     return s, amp * gmask, np.ascontiguousarray(opd_full, dtype=float)
+
+
+def _device_field(pupil):
+    """(slice, amp_eff, opd) of ``dense_field`` with amp_eff and opd as CUDA
+    tensors.  A frozen plane cannot change its amplitude or OPD (lentil's
+    freeze contract), so its merged field is kept on the device with the
+    plane and later calls reuse it (keyed on the mask object as well)."""
+    frozen = bool(getattr(pupil, 'frozen', False))
+    key = id(getattr(pupil, '_mask', None))
+    cache = getattr(pupil, '_lgb_device_field', None) if frozen else None
+    if cache is not None and cache[0] == key:
+        return cache[1]
+    s, amp_eff, opd = dense_field(pupil)
+    shp = (1,) + amp_eff.shape
+    field = (s, dv.to_device(amp_eff, torch.float64).reshape(shp),
+             dv.to_device(opd, torch.float64).reshape(shp))
+    if frozen:
+        try:
+            pupil._lgb_device_field = (key, field)
+        except AttributeError:           # a plane class with __slots__: no cache
+            pass
+    return field
 
 
 def broadband_psf(pupil, wavelengths, weights, pixelscale, shape=None, prop_shape=None,
@@ -280,8 +301,8 @@ def broadband_psf(pupil, wavelengths, weights, pixelscale, shape=None, prop_shap
         img = dev_out
         return _deliver(img, out, tensor_io)
 
-    s, amp_eff, opd = dense_field(pupil)
-    plane_shape = amp_eff.shape
+    s, a, o = _device_field(pupil)
+    plane_shape = tuple(a.shape[1:])
     geo = plan_geometry(plane_shape, s, list(pupil.tilt), pupil.pixelscale, pupil.focal_length,
                         pupil.ptype, wavelengths, pixelscale, shape, prop_shape, oversample, mask)
     dev = dv.device()
@@ -290,8 +311,6 @@ def broadband_psf(pupil, wavelengths, weights, pixelscale, shape=None, prop_shap
     if not geo.keep:
         return _deliver(img, out, tensor_io)
     plan = _cached_plan(geo, precision)
-    a = dv.to_device(amp_eff, torch.float64).reshape((1,) + plane_shape)
-    o = dv.to_device(opd, torch.float64).reshape((1,) + plane_shape)
     w = dv.to_device(weights[geo.keep], torch.float64).reshape(1, -1)
     plan.execute(a, o, w, out=img.reshape((1,) + geo.shape_out), accumulate=True)
     return _deliver(img, out, tensor_io)

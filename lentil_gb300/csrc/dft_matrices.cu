@@ -49,7 +49,10 @@ int launch_dft_matrix_c128(const PhaseAxis& ax, int len_in, int len_out, double2
 // written as 8-byte stores to the four places a block embedding holds them
 // ([Re | -Im] and [Im | Re] rows).  The negated imaginary part is the split
 // of the imaginary part with the sign bits flipped (round-to-nearest is
-// symmetric, so this equals splitting -Im).
+// symmetric, so this equals splitting -Im).  (The SFU sine in place of
+// sincospif for the bf16 form was tried: it moved a bf16 golden case from
+// just under its bound to 2.1e-6, for little speed, the build being near the
+// HBM rate already.)
 constexpr int SPLIT_PER_THREAD = 4;
 constexpr int SPLIT_THREADS = 128;
 

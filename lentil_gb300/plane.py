@@ -158,6 +158,7 @@ class _PlaneBase:
 
     def thaw(self):
         self._frozen = False
+        self.__dict__.pop('_lgb_device_field', None)    # device copy kept while frozen
 
 
 class Plane(_PlaneBase):

@@ -316,3 +316,33 @@ def test_zero_field_blocks_are_skipped_exactly(cuda_device, tile):
     with lg.tuner.forced(tile):
         img = lg.broadband_psf(pl, wl, wt, precision='split-bf16', **kw)
     assert lo.peak_normalised_error(img, ref) < 2e-6
+
+
+def test_frozen_pupil_keeps_its_field_on_the_device(cuda_device):
+    # a frozen pupil's merged field is cached on the device across broadband
+    # calls; thawing drops it, so a changed OPD is seen after re-freezing
+    rng = np.random.default_rng(23)
+    segs = lg.hex_segments(rings=1, seg_radius=18, seg_gap=2)
+    mask = np.asarray([lg.pad(s_, (128, 128)) for s_ in segs])
+    amp = lg.normalize_power(mask.sum(axis=0))
+    opd1 = lg.zernike_compose(amp > 0, np.r_[0, rng.normal(0, 40e-9, 10)])
+    opd2 = lg.zernike_compose(amp > 0, np.r_[0, rng.normal(0, 40e-9, 10)])
+    wl, wt = np.linspace(500e-9, 800e-9, 3), np.array([0.3, 0.4, 0.3])
+    kw = dict(shape=32, oversample=2, precision='fp64')
+
+    def ref(opd):
+        po = lo.Pupil(amplitude=amp, opd=opd, mask=mask, pixelscale=1 / 128, focal_length=10)
+        return lo.broadband_psf(po, wl, wt, 5e-6, shape=32, oversample=2)
+
+    p = lg.Pupil(amplitude=amp, opd=opd1, mask=mask, pixelscale=1 / 128, focal_length=10)
+    p.freeze()
+    first = lg.broadband_psf(p, wl, wt, 5e-6, **kw)
+    assert getattr(p, '_lgb_device_field', None) is not None
+    again = lg.broadband_psf(p, wl, wt, 5e-6, **kw)
+    assert np.array_equal(first, again)
+    assert lo.peak_normalised_error(first, ref(opd1)) < 1e-12
+    p.thaw()
+    assert getattr(p, '_lgb_device_field', None) is None
+    p.opd = opd2
+    p.freeze()
+    assert lo.peak_normalised_error(lg.broadband_psf(p, wl, wt, 5e-6, **kw), ref(opd2)) < 1e-12
