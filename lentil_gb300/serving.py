@@ -278,9 +278,16 @@ class _Slot:
             g = b.graphs.get(tile)
             if reuse and g is None and (tile != 0 or self.tile_decided(b)):
                 b.launch(self)                       # warm-up outside capture
+                # capture_begin/end rather than the torch.cuda.graph context,
+                # whose entry synchronises the device, collects garbage and
+                # empties the caching allocator: the scheduling thread would
+                # wait for every launch in flight
                 g = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(g, stream=stream):
+                g.capture_begin(capture_error_mode='thread_local')
+                try:
                     b.launch(self)
+                finally:
+                    g.capture_end()
                 b.graphs[tile] = g
             if g is not None:
                 g.replay()
@@ -447,19 +454,19 @@ class PSFServer:
                 err = None
             except Exception as e:                     # device timeout or CUDA error
                 err = e
+            hout, b.hout = b.hout, None
+            b.busy = False
+            slot.inflight -= 1
+            self._free_streams.append(si)
+            self.stats['completed'] += len(reqs)      # before any future completes
             for k, r in enumerate(reqs):
                 r.t_done = now
                 if r.future.done():
                     continue
                 if err is None:
-                    r.future.set_result(b.hout[k].numpy())
+                    r.future.set_result(hout[k].numpy())
                 else:
                     r.future.set_exception(err)
-            b.hout = None
-            b.busy = False
-            slot.inflight -= 1
-            self._free_streams.append(si)
-            self.stats['completed'] += len(reqs)
         return bool(done)
 
     def _make_room(self, need):
@@ -521,17 +528,17 @@ class PSFServer:
                         if req in self._queue:
                             self._queue.remove(req)
                     req.t_done = time.perf_counter()
-                    req.future.set_exception(e)
                     self.stats['failed'] += 1
+                    req.future.set_exception(e)
                     progressed = True
                     continue
                 if isinstance(slot, str):             # 'too_big' or 'empty'
                     with self._cv:
                         self._queue.remove(req)
                     if slot == 'too_big':
+                        self.stats['rejected'] += 1
                         req.future.set_exception(MemoryError(
                             'request needs more device memory than the server budget'))
-                        self.stats['rejected'] += 1
                     else:
                         req.t_done = time.perf_counter()
                         req.future.set_result(np.zeros((req.det_shape * req.oversample,) * 2))
@@ -570,10 +577,10 @@ class PSFServer:
                 slot.inflight -= 1
                 self._free_streams.append(si)
                 now = time.perf_counter()
+                self.stats['failed'] += len(batch)
                 for r in batch:
                     r.t_done = now
                     r.future.set_exception(e)
-                self.stats['failed'] += len(batch)
                 progressed = True
                 continue
             self._inflight.append((ev, slot, b, batch, si))
