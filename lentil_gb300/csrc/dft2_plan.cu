@@ -369,11 +369,12 @@ extern "C" int lgb_dft2_plan_execute(lgb_dft2_plan P, const lgb_c128* f, int cou
     return launch_zgemm(M, N, m, P->E1, m, 0, w.T, N, sT, Fout, N, sF, count, P->scale, s);
   }
   const bool bf16 = P->precision == LGB_SPLIT_BF16;
-  if ((st = launch_maxabs_c128_batch(fin, m * n, count, w.maxabs, s))) return st;
+  float* const maxabs = bf16 ? nullptr : w.maxabs;     // bf16: no per-field scale
+  if (maxabs && (st = launch_maxabs_c128_batch(fin, m * n, count, maxabs, s))) return st;
   SplitFieldArgs fa{};
   fa.field = fin;
   fa.m = m; fa.n = n; fa.kp = P->kp1; fa.L = 1; fa.batch = count;
-  fa.maxabs = w.maxabs;
+  fa.maxabs = maxabs;
   fa.hi = w.fh; fa.lo = w.fl;
   if ((st = launch_split_field_T(fa, bf16, s))) return st;
   SplitMftProblem p{};
@@ -381,7 +382,7 @@ extern "C" int lgb_dft2_plan_execute(lgb_dft2_plan P, const lgb_c128* f, int cou
   p.bf16 = bf16;
   p.e1_hi = P->e1h; p.e1_lo = P->e1l; p.f_hi = w.fh; p.f_lo = w.fl;
   p.e2_hi = P->e2h; p.e2_lo = P->e2l; p.g_hi = w.gh; p.g_lo = w.gl;
-  p.maxabs = w.maxabs;
+  p.maxabs = maxabs;
   p.epilogue = 1;
   p.unit2 = P->unit2;
   p.out = reinterpret_cast<double*>(Fout);

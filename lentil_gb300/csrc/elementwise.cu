@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
   const int rtile = blockIdx.x / groups, g = blockIdx.x - rtile * groups;   // row tile, group
   const int rt = rtile * TR, ct = blockIdx.y * TC;
   const int b = blockIdx.z;                                                 // PSF
-  const float sf = pow2_scale_for(a.maxabs[b]);
+  const float sf = a.maxabs ? pow2_scale_for(a.maxabs[b]) : 1.f;   // none: unscaled (bf16)
 
   // thread (w, lane) owns field column ct + lane and rows rt + 8w .. 8w+7:
   // each global load instruction reads 32 consecutive columns of one row,

@@ -37,7 +37,7 @@ struct SplitFieldArgs {
   const double2* field;    // [batch][m][n] complex128 (L 1)
   // common
   int m, n, kp, L, batch;
-  const float* maxabs;     // [batch] max |component| of the field (device)
+  const float* maxabs;     // [batch] max |component| of the field (device), or null: no scale
   uint16_t* hi;            // [batch*L][n][2*kp]
   uint16_t* lo;
   const int* lam_idx;      // optional [L] device: wavelength -> khalf slot
@@ -103,7 +103,7 @@ struct SplitMftProblem {
   bool bf16;
   const uint16_t *e1_hi, *e1_lo, *f_hi, *f_lo, *e2_hi, *e2_lo;
   uint16_t *g_hi, *g_lo;   // stage-1 output / stage-2 A operand
-  const float* maxabs;     // [batch], max |component| of the unscaled field
+  const float* maxabs;     // [batch], max |component| of the unscaled field, or null: no scale
   // stage-2 epilogue
   int epilogue;            // 0: weighted intensity reduced into wbuf, 1: complex128 out
   const double* weights;   // [batch][L] (intensity) -- may be null (weight 1)

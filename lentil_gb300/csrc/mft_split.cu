@@ -114,7 +114,7 @@ struct Params {
   float sG;                  // stage-2 operand scale (power of two)
   uint16_t* g_hi;
   uint16_t* g_lo;
-  const float* maxabs;       // [batch]
+  const float* maxabs;       // [batch], or null (operands not scaled)
   int epilogue;              // stage 2: 0 intensity, 1 complex
   const double* weights;     // [batch][L] or null
   const double* unit2;       // [L]
@@ -492,7 +492,7 @@ __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int
   constexpr int HALF = RUN / 2;
   const int lane = row & 31;
   const int u = w.tm * BM + row, u0 = u - lane;
-  const float sf = pow2_scale_for(p.maxabs[w.psf]);
+  const float sf = p.maxabs ? pow2_scale_for(p.maxabs[w.psf]) : 1.f;   // none: unscaled (bf16)
   const int v0 = w.tn * (BN / 2) + ch * HALF;
   if (p.epilogue == 0) {
     const float inv = 1.f / (sf * p.sG);

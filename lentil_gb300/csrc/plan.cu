@@ -159,11 +159,14 @@ int lgb::dft2_batch(const double2* fin, int count, int m, int n, double2* Fout, 
   LGB_CUDA(cudaMemcpyAsync(w.axes, axes, sizeof(axes), cudaMemcpyHostToDevice, s));
   if ((st = launch_e1_block_split(w.axes, 1, m, M, kp1, cdiv(M, 64) * 128, bf16, w.e1h, w.e1l, s))) return st;
   if ((st = launch_e2_block_split(w.axes + 1, 1, n, N, kp2, cdiv(N, 128) * 256, bf16, w.e2h, w.e2l, s))) return st;
-  if ((st = launch_maxabs_c128_batch(fin, m * n, count, w.maxabs, s))) return st;
+  // bf16 keeps FP32's exponent range: no per-field scale is needed (and a
+  // power-of-two scale would change no result), so only fp16 reduces max|f|
+  float* const maxabs = bf16 ? nullptr : w.maxabs;
+  if (maxabs && (st = launch_maxabs_c128_batch(fin, m * n, count, maxabs, s))) return st;
   SplitFieldArgs fa{};
   fa.field = fin;
   fa.m = m; fa.n = n; fa.kp = kp1; fa.L = 1; fa.batch = count;
-  fa.maxabs = w.maxabs;
+  fa.maxabs = maxabs;
   fa.hi = w.fh; fa.lo = w.fl;
   if ((st = launch_split_field_T(fa, bf16, s))) return st;
   const double one = 1.0;
@@ -173,7 +176,7 @@ int lgb::dft2_batch(const double2* fin, int count, int m, int n, double2* Fout, 
   p.bf16 = bf16;
   p.e1_hi = w.e1h; p.e1_lo = w.e1l; p.f_hi = w.fh; p.f_lo = w.fl;
   p.e2_hi = w.e2h; p.e2_lo = w.e2l; p.g_hi = w.gh; p.g_lo = w.gl;
-  p.maxabs = w.maxabs;
+  p.maxabs = maxabs;
   p.epilogue = 1;
   p.unit2 = w.unit2;
   p.out = reinterpret_cast<double*>(Fout);
@@ -507,13 +510,16 @@ static int psf_execute_n(lgb_psf_plan P, int B, const int* lam_idx, int n_sel, c
   if (is_split(d.precision)) {
     const bool bf16 = d.precision == LGB_SPLIT_BF16;
     cudaEvent_t ev[2];
-    if ((st = launch_maxabs_amp(amp, B, d.H, d.W, d.r0, d.c0, d.m, d.n, ops.maxabs, s))) return st;
+    // bf16: no per-PSF scale (see lgb_dft2_batch)
+    float* const maxabs = bf16 ? nullptr : ops.maxabs;
+    if (maxabs && (st = launch_maxabs_amp(amp, B, d.H, d.W, d.r0, d.c0, d.m, d.n, maxabs, s)))
+      return st;
     SplitFieldArgs fa{};
     fa.amp = amp; fa.opd = opd;
     fa.H = d.H; fa.W = d.W; fa.r0 = d.r0; fa.c0 = d.c0;
     fa.khalf = P->khalf;
     fa.m = d.m; fa.n = d.n; fa.kp = P->kp1; fa.L = L; fa.batch = B;
-    fa.maxabs = ops.maxabs;
+    fa.maxabs = maxabs;
     fa.hi = ops.fh; fa.lo = ops.fl;
     fa.lam_idx = lam_idx;
     fa.kflags = ops.kflags; fa.kf_pitch = ops.kf_pitch;
@@ -527,7 +533,7 @@ static int psf_execute_n(lgb_psf_plan P, int B, const int* lam_idx, int n_sel, c
     p.L_bank = d.n_wavelengths;
     p.e1_hi = P->e1h; p.e1_lo = P->e1l; p.f_hi = ops.fh; p.f_lo = ops.fl;
     p.e2_hi = P->e2h; p.e2_lo = P->e2l; p.g_hi = ops.gh; p.g_lo = ops.gl;
-    p.maxabs = ops.maxabs;
+    p.maxabs = maxabs;
     p.epilogue = 0;
     p.weights = weights;
     p.unit2 = P->unit2;
