@@ -73,13 +73,15 @@ constexpr int EPI_WARPS = 8;
 constexpr int NUM_THREADS = 64 + 32 * EPI_WARPS;
 constexpr uint32_t STG_BYTES = 4096;                       // output staging per epilogue warp
 constexpr unsigned long long WAIT_NS = 2000000000ull;      // default 2 s bound on any wait
-// K blocks per accumulator drain: 2 for bf16 operands (the fast form: half
-// the drains, and twice the MMA run-ahead across an item's output pass), 1
-// for fp16 (the accurate form: the shortest round-toward-zero chains).
-template <bool BF16>
-struct Drain {
-  static constexpr int KB = BF16 ? 2 : 1;
-};
+// K blocks per accumulator drain (the kernel's KB template argument): 2 for
+// bf16 operands when every PSF of the launch carries many wavelengths (the
+// fast form: half the drains, and twice the MMA run-ahead across an item's
+// output pass; the longer chains' round-toward-zero bias is left in, while
+// the band averages the representation error down), 1 otherwise and always
+// for fp16 (the shortest round-toward-zero chains).  A compile-time value:
+// the single MMA-issuing thread is on the critical path, and runtime chain
+// bookkeeping in its loop measurably slowed the pipe.
+constexpr int CHAIN2_MIN_WAVELENGTHS = 16;     // wavelengths per PSF for 2-block bf16 chains
 
 // Pair-tile width: 256 output columns (the fast shape for large transforms:
 // each A tile feeds twice the MMA work) or 128 (twice the tiles, for launches
@@ -533,7 +535,7 @@ __device__ __forceinline__ void write_stage2(const Params& p, const Item& w, int
 }
 
 // -------------------------------------------------------------- kernel ---
-template <bool BF16, int BN>
+template <bool BF16, int BN, int KB>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant__ CUtensorMap tmA_lo,
                  const __grid_constant__ CUtensorMap tmB_hi, const __grid_constant__ CUtensorMap tmB_lo,
@@ -642,8 +644,8 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
           for (int kb = 0; kb < p.kblocks; ++kb) {
             if (!is_live(lv, kb)) continue;
             const int s = it % STAGES, xb = gi & 1;
-            const bool first = j % Drain<BF16>::KB == 0;
-            const bool last = j % Drain<BF16>::KB == Drain<BF16>::KB - 1 || j == lv.n - 1;
+            const bool first = j % KB == 0;
+            const bool last = j % KB == KB - 1 || j == lv.n - 1;
             if (!mbar_wait(full_bar(s), (it / STAGES) & 1, p.err, p.wait_ns)) { ok = false; break; }
             // accumulator xb was drained by both CTAs (its previous group, gi - 2)
             if (first && !mbar_wait(acc_empty(xb), ((gi >> 1) & 1) ^ 1, p.err, p.wait_ns)) { ok = false; break; }
@@ -691,7 +693,7 @@ split_mft_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_consta
       Item w = decode(p, i);
       // accumulator groups of the item (none when its field tile is zero:
       // the output tile is then written as zeros)
-      const int groups = (live_kblocks<BN>(p, w).n + Drain<BF16>::KB - 1) / Drain<BF16>::KB;
+      const int groups = (live_kblocks<BN>(p, w).n + KB - 1) / KB;
       w.tm = 2 * w.tm + (int)rank;           // this CTA's 128-row tile
       float run[C::RUN];
 #pragma unroll
@@ -814,12 +816,12 @@ static cudaLaunchConfig_t pair_config(uint32_t smem, cudaStream_t s, cudaLaunchA
   return cfg;
 }
 
-template <bool BF16, int BN>
+template <bool BF16, int BN, int KB>
 static cudaError_t set_smem_attr() {
   static std::once_flag once;
   static cudaError_t err = cudaSuccess;
   std::call_once(once, [] {
-    err = cudaFuncSetAttribute(split_mft_kernel<BF16, BN>,
+    err = cudaFuncSetAttribute(split_mft_kernel<BF16, BN, KB>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)TileCfg<BN>::SMEM_BYTES);
   });
@@ -827,43 +829,45 @@ static cudaError_t set_smem_attr() {
 }
 
 // Largest number of CTA pairs of this kernel resident at once (per device).
-template <bool BF16, int BN>
+template <bool BF16, int BN, int KB>
 static int max_pairs() {
   static std::mutex mu;
   static int cached[64] = {0};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  if (set_smem_attr<BF16, BN>() != cudaSuccess) return 0;
+  if (set_smem_attr<BF16, BN, KB>() != cudaSuccess) return 0;
   std::lock_guard<std::mutex> lock(mu);
   if (cached[dev] == 0) {
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = pair_config(TileCfg<BN>::SMEM_BYTES, 0, attr);
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, split_mft_kernel<BF16, BN>, &cfg) != cudaSuccess) n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, split_mft_kernel<BF16, BN, KB>, &cfg) != cudaSuccess) n = 0;
     cached[dev] = n;
   }
   return cached[dev];
 }
 
-template <bool BF16, int BN>
+template <bool BF16, int BN, int KB>
 static int launch_one(const Params& p, const CUtensorMap& a_hi, const CUtensorMap& a_lo,
                       const CUtensorMap& b_hi, const CUtensorMap& b_lo, const CUtensorMap& c0,
                       const CUtensorMap& c1, cudaStream_t s) {
-  LGB_CUDA((set_smem_attr<BF16, BN>()));
+  LGB_CUDA((set_smem_attr<BF16, BN, KB>()));
   if (p.n_items <= 0) return LGB_OK;
-  const int pairs = max_pairs<BF16, BN>();
+  const int pairs = max_pairs<BF16, BN, KB>();
   LGB_REQUIRE(pairs > 0, LGB_ECUDA, "split mft: no CTA pair of the tensor-core kernel fits on this GPU");
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = pair_config(TileCfg<BN>::SMEM_BYTES, s, attr);
   cfg.gridDim = dim3(2 * std::min(p.n_items, pairs));
-  LGB_CUDA(cudaLaunchKernelEx(&cfg, split_mft_kernel<BF16, BN>, a_hi, a_lo, b_hi, b_lo, c0, c1, p));
+  LGB_CUDA(cudaLaunchKernelEx(&cfg, split_mft_kernel<BF16, BN, KB>, a_hi, a_lo, b_hi, b_lo, c0, c1, p));
   return LGB_OK;
 }
 
 template <int BN>
-static int launch_stage(const Params& p, bool bf16, const CUtensorMap* m, cudaStream_t s) {
-  return bf16 ? launch_one<true, BN>(p, m[0], m[1], m[2], m[3], m[4], m[5], s)
-              : launch_one<false, BN>(p, m[0], m[1], m[2], m[3], m[4], m[5], s);
+static int launch_stage(const Params& p, bool bf16, bool chain2, const CUtensorMap* m,
+                        cudaStream_t s) {
+  if (!bf16) return launch_one<false, BN, 1>(p, m[0], m[1], m[2], m[3], m[4], m[5], s);
+  return chain2 ? launch_one<true, BN, 2>(p, m[0], m[1], m[2], m[3], m[4], m[5], s)
+                : launch_one<true, BN, 1>(p, m[0], m[1], m[2], m[3], m[4], m[5], s);
 }
 
 // Work items and K blocks of each stage at tile width bn.
@@ -925,6 +929,8 @@ static int run_split_mft(const SplitMftProblem& q, cudaEvent_t* ev, cudaStream_t
       return st;
   }
 
+  // two-block accumulator chains for bf16 PSFs of many wavelengths only
+  const bool chain2 = q.bf16 && q.L >= CHAIN2_MIN_WAVELENGTHS;
   Params p{};
   p.stage = 1;
   p.wait_ns = WAIT_NS;
@@ -955,7 +961,7 @@ static int run_split_mft(const SplitMftProblem& q, cudaEvent_t* ev, cudaStream_t
     p.kf_pitch = q.kf_pitch;
   }
   if (ev) LGB_CUDA(cudaEventRecord(ev[0], s));
-  if ((st = launch_stage<BN>(p, q.bf16, m1, s))) return st;
+  if ((st = launch_stage<BN>(p, q.bf16, chain2, m1, s))) return st;
   if (ev) LGB_CUDA(cudaEventRecord(ev[1], s));
 
   p.stage = 2;
@@ -975,7 +981,7 @@ static int run_split_mft(const SplitMftProblem& q, cudaEvent_t* ev, cudaStream_t
   p.out = q.out;
   p.cscale = q.complex_scale;
   if (ev) LGB_CUDA(cudaEventRecord(ev[2], s));
-  if ((st = launch_stage<BN>(p, q.bf16, m2, s))) return st;
+  if ((st = launch_stage<BN>(p, q.bf16, chain2, m2, s))) return st;
   if (ev) LGB_CUDA(cudaEventRecord(ev[3], s));
   return LGB_OK;
 }
@@ -1071,8 +1077,12 @@ static int run_tile(const SplitMftProblem& q, int bn, cudaEvent_t* ev, cudaStrea
 // Loads and configures both widths' kernels (lazy module load, shared-memory
 // attribute, occupancy) so that no trial is timed across that set-up.
 static void prepare_widths(bool bf16) {
-  if (bf16) { max_pairs<true, 256>(); max_pairs<true, 128>(); }
-  else { max_pairs<false, 256>(); max_pairs<false, 128>(); }
+  if (bf16) {
+    max_pairs<true, 256, 1>(); max_pairs<true, 128, 1>();
+    max_pairs<true, 256, 2>(); max_pairs<true, 128, 2>();
+  } else {
+    max_pairs<false, 256, 1>(); max_pairs<false, 128, 1>();
+  }
 }
 
 // Width for this launch; ev[0..1] are set when the launch is to be timed
