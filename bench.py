@@ -866,7 +866,6 @@ def run_serving_rates(srv, make_request, rng, rates, duration, max_requests):
         reqs = []
         t0 = time.perf_counter()
         t_next = t0
-        n_ev = len(srv.events)
         while t_next - t0 < duration and len(reqs) < max_requests:
             now = time.perf_counter()
             if now < t_next:
@@ -882,7 +881,8 @@ def run_serving_rates(srv, make_request, rng, rates, duration, max_requests):
         lat = np.array([1e3 * r.latency for r in reqs])
         wait = np.array([1e3 * r.queue_wait for r in reqs if r.t_launch is not None])
         svc = np.array([1e3 * (r.t_done - r.t_launch) for r in reqs if r.t_launch is not None])
-        builds = [e for e in srv.events[n_ev:] if e[1] == 'build']
+        window = [e for e in list(srv.events) if e[0] >= t0]
+        builds = [e for e in window if e[1] == 'build']
         worst = sorted(reqs, key=lambda r: -r.latency)[:3]
         results.append({
             'rate_per_s': rate, 'requests': len(reqs), 'window_s': t_next - t0,
@@ -893,7 +893,7 @@ def run_serving_rates(srv, make_request, rng, rates, duration, max_requests):
             'service_p50_ms': float(np.percentile(svc, 50)) if len(svc) else None,
             'service_p99_ms': float(np.percentile(svc, 99)) if len(svc) else None,
             'plan_builds': len(builds), 'plan_build_ms': 1e3 * sum(e[2] for e in builds),
-            'evictions': sum(1 for e in srv.events[n_ev:] if e[1] == 'evict'),
+            'evictions': sum(1 for e in window if e[1] == 'evict'),
             'slowest': [{'latency_ms': 1e3 * r.latency, 'queue_wait_ms': 1e3 * (r.queue_wait or 0),
                          'request': list(r.tag)} for r in worst]})
         done.extend(reqs)

@@ -306,6 +306,7 @@ class PSFServer:
     matrices; default 128 points over 400-1000 nm."""
 
     SHARED_TILE = 256     # tile width of launches issued while others are in flight
+    EVENTS = 4096         # plan build / eviction records kept
 
     def __init__(self, hbm_budget=None, streams=4, max_batch=4, precision='split',
                  use_graphs=True, grid=None, device=None, tuner_cache=None):
@@ -334,9 +335,9 @@ class PSFServer:
         self._streams = []
         self._stop = False
         self.stats = collections.Counter()
-        # (perf_counter time, kind, value): 'build' (plan build seconds on the
-        # scheduler thread), 'evict' (plan bytes released)
-        self.events = []
+        # the last EVENTS (perf_counter time, kind, value): 'build' (plan
+        # build seconds on the scheduler thread), 'evict' (plan bytes released)
+        self.events = collections.deque(maxlen=self.EVENTS)
         self._thread = threading.Thread(target=self._loop, name='psf-server', daemon=True)
         self._thread.start()
 
