@@ -58,6 +58,10 @@ def parse():
                     help='serving: at most this many requests per rate')
     ap.add_argument('--serve-warm', type=float, default=4.0,
                     help='serving: seconds of the warm pass at 100 requests/s')
+    ap.add_argument('--serve-streams', type=int, default=4,
+                    help='serving: CUDA streams of the server (launches in flight)')
+    ap.add_argument('--serve-batch', type=int, default=8,
+                    help='serving: requests batched into one launch at most')
     ap.add_argument('--serving-leg', type=int, default=1,
                     help='default workload: 1 = add a short serving leg (p50/p99) to the line')
     ap.add_argument('--serving-leg-rates', default='200,1000',
@@ -937,7 +941,8 @@ def run_serving_leg(args):
     rng = np.random.default_rng(3)
     grid = np.linspace(400e-9, 1000e-9, 128)
     rates = [float(r) for r in args.serving_leg_rates.split(',')]
-    with serving.PSFServer(streams=4, max_batch=4, precision=args.precision, grid=grid) as srv:
+    with serving.PSFServer(streams=args.serve_streams, max_batch=args.serve_batch,
+                           precision=args.precision, grid=grid) as srv:
         make_request = serving_requests(rng, grid, server=srv)
         run_serving_rates(srv, make_request, rng, [100.0], 4.0, 400)
         res, done = run_serving_rates(srv, make_request, rng, rates, 3.0, 600)
@@ -957,7 +962,8 @@ def run_serving(args):
     rng = np.random.default_rng(3)
     grid = np.linspace(400e-9, 1000e-9, 128)
     rates = [float(r) for r in args.rates.split(',')]
-    with serving.PSFServer(streams=4, max_batch=4, precision=args.precision, grid=grid) as srv:
+    with serving.PSFServer(streams=args.serve_streams, max_batch=args.serve_batch,
+                           precision=args.precision, grid=grid) as srv:
         make_request = serving_requests(rng, grid, server=srv)
         # warm pass: every geometry's plan built and the tile widths tuned
         # before the measured rates (plan builds are reported per rate)
@@ -984,7 +990,8 @@ def run_serving(args):
                                    'and Zernike bases resident on the server, requests carry '
                                    'coefficients (host_arrays_100_per_s: requests carrying '
                                    'amplitude and OPD arrays)',
-                       'streams': 4, 'max_batch': 4, 'duration_s_per_rate': args.duration,
+                       'streams': args.serve_streams, 'max_batch': args.serve_batch,
+                       'duration_s_per_rate': args.duration,
                        'max_requests_per_rate': args.max_requests,
                        'mft_tile': tuner_summary(args)}}
     print(json.dumps(line), flush=True)

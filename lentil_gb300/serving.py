@@ -308,7 +308,7 @@ class PSFServer:
     SHARED_TILE = 256     # tile width of launches issued while others are in flight
     EVENTS = 4096         # plan build / eviction records kept
 
-    def __init__(self, hbm_budget=None, streams=4, max_batch=4, precision='split',
+    def __init__(self, hbm_budget=None, streams=4, max_batch=8, precision='split',
                  use_graphs=True, grid=None, device=None, tuner_cache=None):
         self.device = device or dv.device()
         self.tuner_cache = tuner_cache       # tile widths loaded now, saved on close
