@@ -628,7 +628,11 @@ def run_gpu(args):
                 'path': 'PSFPlan.execute on pinned-host amp/opd/weights copied in and the '
                         'images copied out every step; copies on a second stream overlap the '
                         'previous/next step\'s compute'},
-        'gpu_launches': 5 * P * args.steps,
+        # the library's kernels in the timed region, from the plan profiler's
+        # launch counts (phasor operand, both MFT stages, window add), plus
+        # the per-PSF max reduction that only the fp16 form launches
+        'gpu_launches': int(sum(kcnt[i] for i in range(4))) +
+                        (P * args.steps if args.precision == 'split-fp16' else 0),
         'clocks': clk.summary(),
     }
     if serving_leg:
