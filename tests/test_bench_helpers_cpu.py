@@ -51,3 +51,34 @@ def test_live_fraction_cases():
     assert bench.stage1_live_fraction(two, 256) == pytest.approx(10 / 84)
     # more than 128 K blocks: the kernel keeps no flags and issues them all
     assert bench.stage1_live_fraction(np.eye(4200, 64, dtype=bool), 256) == 1.0
+
+
+def test_sample_indices_spread_and_rotate():
+    # the reference arm's per-step wavelength samples: n indices spread over
+    # the band, shifted by one per step, always inside it
+    a = bench.sample_indices(64, 4, 0)
+    assert list(a) == [0, 16, 32, 48]
+    seen = set()
+    for k in range(64):
+        idx = bench.sample_indices(64, 4, k)
+        assert len(set(idx)) == 4 and idx.min() >= 0 and idx.max() < 64
+        seen.update(idx.tolist())
+    assert seen == set(range(64))
+    assert list(bench.sample_indices(3, 5, 0)) == [0, 1, 2, 3 % 3, 4 % 3]
+
+
+def test_reference_module_falls_back_to_the_port(monkeypatch, tmp_path):
+    # without lentil installed beside the repository the CPU legs run the
+    # numpy restatement under oracle/ and say so
+    monkeypatch.setattr(bench, 'LENTIL_DIR', str(tmp_path))
+    mod, kind, label = bench.reference_module()
+    assert kind == 'port' and 'oracle' in label
+    for name in ('Pupil', 'Wavefront', 'propagate_dft'):
+        assert hasattr(mod, name)
+
+
+def test_reference_module_uses_lentil_when_installed():
+    if not os.path.isfile(os.path.join(bench.LENTIL_DIR, 'lentil', '__init__.py')):
+        pytest.skip('lentil is not installed under baseline/_ref')
+    mod, kind, label = bench.reference_module()
+    assert kind == 'reference' and mod.__version__ in label
