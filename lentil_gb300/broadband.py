@@ -122,8 +122,8 @@ class PSFPlan:
         # mapping new device memory; executes on other streams are recorded
         # on the block so that it outlives their work
         nbytes = lib.lgb_psf_plan_size(ctypes.byref(d))
-        if nbytes == 0:
-            _lib.check(lib.lgb_psf_plan_create(ctypes.byref(d), None, None))   # raises the reason
+        if nbytes == 0:                  # an invalid description: the size call recorded why
+            _lib.check(_lib.EINVAL)
         self._home = torch.cuda.current_stream()
         self._foreign = set()
         self._mem = dv.workspace(nbytes)

@@ -124,3 +124,24 @@ def test_no_cpu_fallback():
                  lambda: lg.zernike_compose(np.ones((8, 8)), [0, 1e-8])):
         with pytest.raises(RuntimeError, match='CUDA device'):
             call()
+
+
+def test_psf_plan_size_rejects_a_bad_description(lib):
+    # lgb_psf_plan_size returns 0 for an invalid description and records the
+    # reason, which the Python plan raises as ValueError (no device needed)
+    lam = np.array([6e-7]); ar = np.array([1e-3]); sh = np.zeros(1)
+    d = _lib.PsfDesc()
+    d.H = d.W = 64
+    d.r0 = d.c0 = 0
+    d.m, d.n = 80, 64                          # field slice taller than the pupil plane
+    d.M = d.N = d.out_rows = d.out_cols = 32
+    d.n_wavelengths = 1
+    d.wavelengths, d.alpha_r, d.alpha_c = lam.ctypes.data, ar.ctypes.data, ar.ctypes.data
+    d.shift_r = d.shift_c = sh.ctypes.data
+    d.batch, d.precision = 1, _lib.SPLIT_BF16
+    assert lib.lgb_psf_plan_size(ctypes.byref(d)) == 0
+    assert b'field slice outside the pupil plane' in lib.lgb_last_error()
+    with pytest.raises(ValueError, match='field slice'):
+        _lib.check(_lib.EINVAL)
+    d.m = 64                                   # valid: a positive size
+    assert lib.lgb_psf_plan_size(ctypes.byref(d)) > 0
