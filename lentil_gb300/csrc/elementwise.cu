@@ -124,8 +124,22 @@ __device__ __forceinline__ void ft_store_4d(const CUtensorMap* map, uint32_t src
       : "memory");
 }
 
+// a read-once stream: no L1 allocation (the block's wavelength loop keeps
+// the values in registers)
+__device__ __forceinline__ double ld_stream(const double* p) {
+  double v;
+  asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+// 1/lambda of wavelength l of the launch as a float-float pair
+__device__ __forceinline__ float2 cycles_per_metre(const SplitFieldArgs& a, int l) {
+  const float2 k2 = a.khalf[a.lam_idx ? a.lam_idx[l] : l];   // 2/lambda
+  return make_float2(0.5f * k2.x, 0.5f * k2.y);
+}
+
 template <bool BF16, bool PHASOR>
-__global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, int groups,
+__global__ void __launch_bounds__(256, BF16 ? 5 : 4) split_field_T_kernel(SplitFieldArgs a, int groups,
                                                             const __grid_constant__ CUtensorMap map_hi,
                                                             const __grid_constant__ CUtensorMap map_lo) {
   extern __shared__ uint8_t ft_smem_raw[];
@@ -144,6 +158,15 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
   // and the thread's 8 values of a plane are one 16-byte chunk of its tile
   // row (chunk w of row lane, swizzled: no bank conflicts)
   const int lane = tid & 31, w = tid >> 5;
+  const int L = PHASOR ? a.L : 1;
+  const int per = (L + groups - 1) / groups;
+  const int l0 = g * per, l1 = min(L, l0 + per);
+  // the block's wavelength factors 1/lambda (a float-float pair: half of the
+  // stored 2/lambda, exact), one per lane for 32 wavelengths at a time and
+  // broadcast by shuffles in the loop, so that no global load waits between
+  // the loop's barriers
+  float2 k_lane = make_float2(0.f, 0.f);
+  if (PHASOR && l0 + lane < l1) k_lane = cycles_per_metre(a, l0 + lane);
   float amp_r[8], o_hi[8], o_lo[8];
   float2 fv[8];
 #pragma unroll
@@ -151,15 +174,20 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
     const int r = rt + 8 * w + k, c = ct + lane;
     amp_r[k] = 0.f; o_hi[k] = 0.f; o_lo[k] = 0.f; fv[k] = make_float2(0.f, 0.f);
     if (r < a.m && c < a.n) {
+      // the conversions are integer operations, not the FP64 pipe (every
+      // wavelength group of a tile repeats them); the amplitude enters
+      // linearly, so its truncated float (2^-23) is far inside the split's
+      // 16 (bf16) or 22 (fp16) bits
       if (PHASOR) {
         const size_t q = ((size_t)b * a.H + (a.r0 + r)) * a.W + (a.c0 + c);
-        const double o = a.opd[q];
-        amp_r[k] = (float)a.amp[q] * sf;
-        o_hi[k] = (float)o;
-        o_lo[k] = (float)(o - (double)o_hi[k]);
+        const float2 o = split_double(ld_stream(a.opd + q));
+        amp_r[k] = truncate_double(ld_stream(a.amp + q)) * sf;
+        o_hi[k] = o.x;
+        o_lo[k] = o.y;
       } else {
         const double2 v = a.field[((size_t)b * a.m + r) * a.n + c];
-        fv[k] = make_float2((float)v.x * sf, (float)v.y * sf);
+        const float2 re = split_double(v.x), im = split_double(v.y);
+        fv[k] = make_float2((re.x + re.y) * sf, (im.x + im.y) * sf);
       }
     }
   }
@@ -185,27 +213,29 @@ __global__ void __launch_bounds__(256) split_field_T_kernel(SplitFieldArgs a, in
     }
   }
 
-  const int L = PHASOR ? a.L : 1;
-  const int per = (L + groups - 1) / groups;
-  const int l0 = g * per, l1 = min(L, l0 + per);
   const uint32_t chunk = (uint32_t)lane * 128u + ((uint32_t)(w ^ (lane & 7)) << 4);
   for (int l = l0; l < l1; ++l) {
     if (PHASOR) {
-      const float2 kk = a.khalf[a.lam_idx ? a.lam_idx[l] : l];   // 2/lambda, float-float pair
+      const int j = (l - l0) & 31;
+      if (j == 0 && l != l0)                         // the next 32 wavelengths (warp-uniform)
+        k_lane = l + lane < l1 ? cycles_per_metre(a, l + lane) : make_float2(0.f, 0.f);
+      const float kx = __shfl_sync(0xffffffffu, k_lane.x, j);
+      const float ky = __shfl_sync(0xffffffffu, k_lane.y, j);
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
-        // x = opd * 2/lambda half-cycles, reduced mod 2 before the sine
-        const float p = o_hi[k] * kk.x;
-        float e = fmaf(o_hi[k], kk.x, -p);
-        e = fmaf(o_hi[k], kk.y, fmaf(o_lo[k], kk.x, e));
-        const float x = (p - 2.f * rintf(0.5f * p)) + e;
+        // t = opd / lambda cycles (float-float product), reduced to
+        // [-1/2, 1/2] before the sine
+        const float p = o_hi[k] * kx;
+        float e = fmaf(o_hi[k], kx, -p);
+        e = fmaf(o_hi[k], ky, fmaf(o_lo[k], kx, e));
+        const float t = (p - rintf(p)) + e;
         float sn, cs;
         if (BF16) {
           // bf16 hi+lo keeps ~16 significant bits (error ~2^-17); the SFU
           // sine's absolute error on [-pi, pi] (~2^-21.4) is far below that
-          __sincosf(x * 3.14159265358979f, &sn, &cs);
+          __sincosf(t * 6.28318530717959f, &sn, &cs);
         } else {
-          sincospif(x, &sn, &cs);        // fp16 hi+lo keeps ~22 bits
+          sincospif(2.f * t, &sn, &cs);  // fp16 hi+lo keeps ~22 bits
         }
         fv[k] = make_float2(amp_r[k] * cs, amp_r[k] * sn);
       }
@@ -256,11 +286,13 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
   // the blocks run in waves of `cap` resident blocks; pick the group count
   // that minimises whole waves times the work of one block (the last wave
   // of a launch is otherwise partly empty), among counts up to 16.  A
-  // block's fixed part (loading amp and opd, the flags) counts as two
-  // wavelengths of work.  A block takes at most 16 wavelengths (when 16
-  // groups allow it), so that no block holds an SM for long: the MFT's
-  // persistent CTA pairs of a launch on another stream start only where an
-  // SM is free, and a late pair delays its whole launch.
+  // block's fixed part (loading and converting amp and opd, the flags)
+  // counts as five wavelengths of work: measured on the 1019 x 941 field at
+  // 64 wavelengths, where 1, 2, 3, 4, 6 and 16 groups ran 0.101, 0.109,
+  // 0.099, 0.112, 0.115 and 0.174 ms.  A block takes at most 32 wavelengths
+  // (when 16 groups allow it), so that no block holds an SM for long: the
+  // MFT's persistent CTA pairs of a launch on another stream start only
+  // where an SM is free, and a late pair delays its whole launch.
   int per_sm = 0;
   auto kfn = bf16 ? (a.amp ? split_field_T_kernel<true, true> : split_field_T_kernel<true, false>)
                   : (a.amp ? split_field_T_kernel<false, true> : split_field_T_kernel<false, false>);
@@ -271,9 +303,9 @@ int launch_split_field_T(const SplitFieldArgs& a, bool bf16, cudaStream_t s) {
   const long long base = std::max(1LL, (long long)spatial * psfs);
   int groups = 1;
   double best = 1e300;
-  for (int g = std::max(1, std::min(cdiv(L, 16), 16)); g <= std::min(L, 16); ++g) {
+  for (int g = std::max(1, std::min(cdiv(L, 32), 16)); g <= std::min(L, 16); ++g) {
     const long long waves = (base * g + cap - 1) / cap;
-    const double cost = (double)waves * (double)(cdiv(L, g) + 2);   // waves x work per block
+    const double cost = (double)waves * (double)(cdiv(L, g) + 5);   // waves x work per block
     if (cost < best * (1.0 - 1e-9)) { best = cost; groups = g; }
   }
   groups = cdiv(L, cdiv(L, groups));                 // no empty trailing group
@@ -336,24 +368,44 @@ int launch_maxabs_c128_batch(const double2* f, int count, int batch, float* out,
 }
 
 // ---------------------------------------------------------------------------
-// FP32 intensity window (reduced into by the tensor-core epilogue) added to
-// the float64 output image
+// FP32 intensity window (reduced into by the tensor-core epilogue) added to,
+// or stored into, the float64 output image.  The widening is done by integer
+// operations (this part's FP64 pipe converts at a small fraction of the
+// FP32 rate): exact for normal floats, infinities and NaNs; zero and
+// subnormal floats (below 1.2e-38) give a signed zero.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ double widen_float(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  if (e == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  // exponent rebiased 127 -> 1023 (255, infinity or NaN, -> 2047);
+  // significand bits 22..3 in the high word, 2..0 at the top of the low word
+  const uint32_t eb = e == 0xFFu ? 0x7FFu : e + 896u;
+  const uint32_t hi = (u & 0x80000000u) | (eb << 20) | ((u & 0x7FFFFFu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+template <bool ADD>
 __global__ void window_add_kernel(const float* __restrict__ wbuf, int M, int N, int ldw,
                                   double* __restrict__ out, int ld_out, long long out_bs,
                                   int win_r0, int win_c0) {
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   const int u = blockIdx.y, b = blockIdx.z;
   if (v >= N || u >= M) return;
-  out[(size_t)b * out_bs + (size_t)(win_r0 + u) * ld_out + win_c0 + v] +=
-      (double)wbuf[((size_t)b * M + u) * ldw + v];
+  double* const o = out + (size_t)b * out_bs + (size_t)(win_r0 + u) * ld_out + win_c0 + v;
+  const double x = widen_float(wbuf[((size_t)b * M + u) * ldw + v]);
+  if (ADD) *o += x;
+  else *o = x;
 }
 
 int launch_window_add(const float* wbuf, int M, int N, int ldw, int batch, double* out, int ld_out,
-                      long long out_bs, int win_r0, int win_c0, cudaStream_t s) {
+                      long long out_bs, int win_r0, int win_c0, bool add, cudaStream_t s) {
   if (M <= 0 || N <= 0 || batch <= 0) return LGB_OK;
   dim3 grid(cdiv(N, 128), M, batch);
-  window_add_kernel<<<grid, 128, 0, s>>>(wbuf, M, N, ldw, out, ld_out, out_bs, win_r0, win_c0);
+  if (add)
+    window_add_kernel<true><<<grid, 128, 0, s>>>(wbuf, M, N, ldw, out, ld_out, out_bs, win_r0, win_c0);
+  else
+    window_add_kernel<false><<<grid, 128, 0, s>>>(wbuf, M, N, ldw, out, ld_out, out_bs, win_r0, win_c0);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }

@@ -25,6 +25,42 @@ __device__ __forceinline__ float pow2_scale_for(float maxabs) {
   return ldexpf(1.f, -e);
 }
 
+// A double as an unevaluated float pair hi + lo, by integer operations only
+// (this part's FP64 pipe runs double<->float conversions at a small
+// fraction of the FP32 rate): hi = d with its significand truncated to 24
+// bits (the funnel shift moves the exponent and top significand bits into
+// float position, the subtraction rebiases the exponent from 1023 to 127),
+// lo = the remaining 29 significand bits, converted to float (rounded to 24
+// bits) and scaled by 2^(exponent - 52), with d's sign.  hi + lo is d to
+// 2^-48 relative for |d| >= 2^-74; below that lo is 0 (hi still exact to
+// 2^-23), and |d| < 2^-126 gives 0.  Non-finite or |d| >= 2^128 take the
+// plain conversion.
+__device__ __forceinline__ float2 split_double(double d) {
+  const uint32_t lo32 = (uint32_t)__double2loint(d), hi32 = (uint32_t)__double2hiint(d);
+  const uint32_t e = (hi32 >> 20) & 0x7FFu;            // biased exponent
+  const uint32_t sign = hi32 & 0x80000000u;
+  if (e < 897u) return make_float2(0.f, 0.f);
+  if (e > 1150u) return make_float2(__double2float_rn(d), 0.f);
+  const uint32_t hb = (__funnelshift_l(lo32, hi32, 3) - (896u << 23)) | sign;
+  float lo = 0.f;
+  if (e >= 949u) {
+    lo = __uint2float_rn(lo32 & 0x1FFFFFFFu) * __uint_as_float((e - 948u) << 23);
+    lo = __uint_as_float(__float_as_uint(lo) | sign);
+  }
+  return make_float2(__uint_as_float(hb), lo);
+}
+
+// The float nearest below |d| in magnitude (significand truncated to 24
+// bits, relative error below 2^-23), by the same integer operations as
+// split_double; |d| < 2^-126 gives 0.
+__device__ __forceinline__ float truncate_double(double d) {
+  const uint32_t lo32 = (uint32_t)__double2loint(d), hi32 = (uint32_t)__double2hiint(d);
+  const uint32_t e = (hi32 >> 20) & 0x7FFu;
+  if (e < 897u) return 0.f;
+  if (e > 1150u) return __double2float_rn(d);
+  return __uint_as_float((__funnelshift_l(lo32, hi32, 3) - (896u << 23)) | (hi32 & 0x80000000u));
+}
+
 // Input of the split operand builder: either a phasor from amplitude/OPD
 // planes (one per PSF, for a list of wavelengths) or a complex field.
 struct SplitFieldArgs {
@@ -128,8 +164,8 @@ inline int kflag_pitch(int kp2) { return 8 * ((kp2 + 255) / 256); }
 int launch_split_mft(const SplitMftProblem& p, cudaStream_t s);
 // scale applied to the stage-1 result before its 16-bit split
 float split_g_scale(int m);
-// out[b][win] += wbuf[b] (FP32 window -> float64 image)
+// out[b][win] += wbuf[b] (add) or out[b][win] = wbuf[b] (FP32 window -> float64 image)
 int launch_window_add(const float* wbuf, int M, int N, int ldw, int batch, double* out, int ld_out,
-                      long long out_bs, int win_r0, int win_c0, cudaStream_t s);
+                      long long out_bs, int win_r0, int win_c0, bool add, cudaStream_t s);
 
 }  // namespace lgb

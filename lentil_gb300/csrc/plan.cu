@@ -505,7 +505,11 @@ static int psf_execute_n(lgb_psf_plan P, int B, const int* lam_idx, int n_sel, c
   cudaStream_t s = as_stream(stream);
   int st;
   const size_t img = (size_t)d.out_rows * d.out_cols;
-  if (!accumulate) LGB_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * img * B, s));
+  // the split path stores its window into a fresh image: only the pixels
+  // outside the window need zeros
+  const bool window_is_image = d.M == d.out_rows && d.N == d.out_cols;
+  if (!accumulate && !(is_split(d.precision) && window_is_image))
+    LGB_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * img * B, s));
   LGB_CUDA(cudaMemsetAsync(errp, 0, sizeof(int), s));
   if (is_split(d.precision)) {
     const bool bf16 = d.precision == LGB_SPLIT_BF16;
@@ -555,7 +559,7 @@ static int psf_execute_n(lgb_psf_plan P, int B, const int* lam_idx, int n_sel, c
     }
     if ((st = prof_begin(P, LGB_PROFILE_OTHER, s, ev))) return st;
     if ((st = launch_window_add(ops.wbuf, d.M, d.N, ops.ldw, B, out, d.out_cols, (long long)img,
-                                d.win_r0, d.win_c0, s)))
+                                d.win_r0, d.win_c0, accumulate != 0, s)))
       return st;
     return prof_end(P, LGB_PROFILE_OTHER, s, ev);
   }

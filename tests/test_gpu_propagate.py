@@ -193,6 +193,39 @@ def test_plan_batch_matches_single(cuda_device):
             assert lo.peak_normalised_error(outb[b], o1[0]) < tol
 
 
+@pytest.mark.parametrize('image,origin', [((80, 72), (0, 0)),        # the window is the image
+                                          ((100, 90), (7, 11))])    # a window inside the image
+def test_plan_output_overwrite_and_accumulate(cuda_device, image, origin):
+    # accumulate=False replaces whatever the output held (a window that
+    # covers the image is stored without clearing it first); accumulate=True
+    # adds the PSF to it
+    rng = np.random.default_rng(12)
+    H = 96
+    amp = lo.normalize_power(lg.circle((H, H), 44))
+    wl = np.linspace(500e-9, 800e-9, 4)
+    alphas = [((1 / 88) * 5e-6 / (l * 10 * 2),) * 2 for l in wl]
+    shifts = [(0.0, 0.0)] * len(wl)
+    A = torch.as_tensor(amp[None].copy(), device='cuda')
+    O = torch.as_tensor(lg.zernike_compose(amp, np.r_[0, rng.normal(0, 30e-9, 10)])[None],
+                        device='cuda')
+    W = torch.as_tensor(rng.uniform(0.5, 1.5, (1, len(wl))), device='cuda')
+    for prec in ('fp64', 'split-bf16'):
+        plan = lg.PSFPlan((H, H), (0, 0, H, H), (0, 0), wl, alphas, shifts, (80, 72), image,
+                          origin, batch=1, precision=prec)
+        fresh = plan.execute(A, O, W).cpu().numpy()
+        assert fresh.shape == (1,) + image
+        r0, c0 = origin
+        outside = np.ones(image, bool)
+        outside[r0:r0 + 80, c0:c0 + 72] = False
+        assert np.all(fresh[0][outside] == 0)
+        garbage = torch.as_tensor(rng.uniform(-5, 5, (1,) + image), device='cuda')
+        over = plan.execute(A, O, W, out=garbage.clone()).cpu().numpy()
+        added = plan.execute(A, O, W, out=garbage.clone(), accumulate=True).cpu().numpy()
+        tol = (1e-13 if prec == 'fp64' else 1e-6) * fresh.max()  # split: FP32 atomics, order not fixed
+        assert np.abs(over - fresh).max() <= tol, prec
+        assert np.abs(added - (garbage.cpu().numpy() + fresh)).max() <= tol + 1e-12, prec
+
+
 @pytest.mark.parametrize('name', ['px64os2', 'px90os3', 'px128os4',          # grid samples
                                   'px100os3', 'px75os2', 'px61os7', 'px128os3', 'px64os5'])
 def test_pixel_pixelate_golden(golden, cuda_device, name):
