@@ -193,6 +193,26 @@ def test_plan_batch_matches_single(cuda_device):
             assert lo.peak_normalised_error(outb[b], o1[0]) < tol
 
 
+def test_broadband_many_wavelengths(cuda_device):
+    # 520 wavelengths: the phasor operand kernel's blocks then take more than
+    # 32 wavelengths each (16 groups at most), so they reload their
+    # wavelength factors part-way through the loop
+    rng = np.random.default_rng(14)
+    H = 40
+    amp = lo.normalize_power(lg.circle((H, H), 18))
+    opd = lg.zernike_compose(amp, np.r_[0, rng.normal(0, 40e-9, 10)])
+    wl = np.linspace(500e-9, 900e-9, 520)
+    wt = rng.uniform(0.5, 1.5, len(wl))
+    wt /= wt.sum()
+    kw = dict(shape=16, oversample=2)
+    po = lo.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 36, focal_length=10)
+    ref = lo.broadband_psf(po, wl, wt, 5e-6, **kw)
+    for prec, tol in (('fp64', 1e-12), ('split-bf16', 2e-6)):
+        pl = lg.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 36, focal_length=10)
+        img = lg.broadband_psf(pl, wl, wt, 5e-6, precision=prec, **kw)
+        assert lo.peak_normalised_error(img, ref) < tol, prec
+
+
 @pytest.mark.parametrize('image,origin', [((80, 72), (0, 0)),        # the window is the image
                                           ((100, 90), (7, 11))])    # a window inside the image
 def test_plan_output_overwrite_and_accumulate(cuda_device, image, origin):
