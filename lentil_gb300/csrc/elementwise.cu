@@ -369,22 +369,9 @@ int launch_maxabs_c128_batch(const double2* f, int count, int batch, float* out,
 
 // ---------------------------------------------------------------------------
 // FP32 intensity window (reduced into by the tensor-core epilogue) added to,
-// or stored into, the float64 output image.  The widening is done by integer
-// operations (this part's FP64 pipe converts at a small fraction of the
-// FP32 rate): exact for normal floats, infinities and NaNs; zero and
-// subnormal floats (below 1.2e-38) give a signed zero.
+// or stored into, the float64 output image (widen_float: integer operations,
+// kernels.cuh).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double widen_float(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t e = (u >> 23) & 0xFFu;
-  if (e == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-  // exponent rebiased 127 -> 1023 (255, infinity or NaN, -> 2047);
-  // significand bits 22..3 in the high word, 2..0 at the top of the low word
-  const uint32_t eb = e == 0xFFu ? 0x7FFu : e + 896u;
-  const uint32_t hi = (u & 0x80000000u) | (eb << 20) | ((u & 0x7FFFFFu) >> 3);
-  return __hiloint2double((int)hi, (int)(u << 29));
-}
-
 template <bool ADD>
 __global__ void window_add_kernel(const float* __restrict__ wbuf, int M, int N, int ldw,
                                   double* __restrict__ out, int ld_out, long long out_bs,

@@ -61,6 +61,20 @@ __device__ __forceinline__ float truncate_double(double d) {
   return __uint_as_float((__funnelshift_l(lo32, hi32, 3) - (896u << 23)) | (hi32 & 0x80000000u));
 }
 
+// float -> double by integer operations (this part's FP64 pipe converts at
+// a small fraction of the FP32 rate): exact for normal floats, infinities
+// and NaNs; zero and subnormal floats (below 1.2e-38) give a signed zero.
+__device__ __forceinline__ double widen_float(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  if (e == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  // exponent rebiased 127 -> 1023 (255, infinity or NaN, -> 2047);
+  // significand bits 22..3 in the high word, 2..0 at the top of the low word
+  const uint32_t eb = e == 0xFFu ? 0x7FFu : e + 896u;
+  const uint32_t hi = (u & 0x80000000u) | (eb << 20) | ((u & 0x7FFFFFu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 // Input of the split operand builder: either a phasor from amplitude/OPD
 // planes (one per PSF, for a list of wavelengths) or a complex field.
 struct SplitFieldArgs {

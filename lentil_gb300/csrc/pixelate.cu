@@ -7,7 +7,8 @@
 //     with C = ifft diag(s) fft real and symmetric (s is real and even), so
 //     each axis is filtered by this file's shared-memory radix-2 FFTs with two
 //     real rows packed into one complex transform (fft, times s, inverse fft:
-//     C a + i C b), between tiled transposes (~5 N^2 log2 N flop);
+//     C a + i C b), between tiled transposes (~5 N^2 log2 N flop), in
+//     double-float arithmetic (below);
 //   - any other N: |C . img . C^T| with C the real symmetric circulant
 //     C[i][j] = c[(i - j) mod N], c = ifft(s), as two FP64 GEMMs.
 // pixelate then resamples by 1/os with a cubic spline (lentil/util.py:261-349);
@@ -84,46 +85,121 @@ __global__ void __launch_bounds__(512) fft_rows_kernel(double2* __restrict__ dat
     row[i] = make_double2(sm[i].x * scale, sm[i].y * scale);
 }
 
+// Double-float arithmetic: a value as the unevaluated sum hi + lo of two
+// floats (about 48 significant bits).  This part's FP64 units retire about
+// two FMAs a clock per SM against 128 FP32 lanes, so the pixel-MTF FFTs run
+// in float pairs: ~90 FP32 operations per radix-2 butterfly in place of ~8
+// FP64 ones, at a rounding error near 2^-47 per operation (the FFT of
+// N <= 8192 points stays near 1e-14 of the signal).  Sums use Knuth's
+// error-free two-sum, products the FMA residual, each renormalised with
+// Dekker's fast two-sum; the _rn intrinsics keep the compiler from fusing
+// the steps whose rounding the transformations rely on.
+struct dfl {
+  float hi, lo;
+};
+__device__ __forceinline__ dfl df_renorm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  return df_renorm(s, e);
+}
+__device__ __forceinline__ dfl df_sub(dfl a, dfl b) { return df_add(a, {-b.hi, -b.lo}); }
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return df_renorm(p, e);
+}
+// a complex double-float value (re.hi, re.lo, im.hi, im.lo) as one float4
+__device__ __forceinline__ float4 df_pack(dfl re, dfl im) { return make_float4(re.hi, re.lo, im.hi, im.lo); }
+
+// exp(-2 pi i k / N), k < N/2, as double-float pairs
+__global__ void twiddle_df_kernel(int N, float4* __restrict__ tw) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N / 2) return;
+  double s, c;
+  sincospi(-2.0 * (double)k / N, &s, &c);
+  const float2 cc = split_double(c), ss = split_double(s);
+  tw[k] = make_float4(cc.x, cc.y, ss.x, ss.y);
+}
+
+// Radix-2 butterflies over a bit-reversed row of complex double-float values
+// in shared memory: natural order out (the caller syncs before; this returns
+// after a final sync).
+__device__ __forceinline__ void fft_stages_df(float4* sm, int N, int logN,
+                                              const float4* __restrict__ tw, bool inverse) {
+  for (int st = 1; st <= logN; ++st) {
+    const int half = 1 << (st - 1);
+    const int stride = N >> st;                        // twiddle index step
+    for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
+      const int pos = b & (half - 1);
+      const int i0 = ((b >> (st - 1)) << st) + pos, i1 = i0 + half;
+      const float4 w4 = tw[pos * stride];
+      const dfl wr{w4.x, w4.y};
+      const dfl wi = inverse ? dfl{-w4.z, -w4.w} : dfl{w4.z, w4.w};
+      const float4 a4 = sm[i0], v4 = sm[i1];
+      const dfl ar{a4.x, a4.y}, ai{a4.z, a4.w}, vr{v4.x, v4.y}, vi{v4.z, v4.w};
+      const dfl tr = df_sub(df_mul(wr, vr), df_mul(wi, vi));
+      const dfl ti = df_add(df_mul(wr, vi), df_mul(wi, vr));
+      sm[i0] = df_pack(df_add(ar, tr), df_add(ai, ti));
+      sm[i1] = df_pack(df_sub(ar, tr), df_sub(ai, ti));
+    }
+    __syncthreads();
+  }
+}
+
 // The pixel MTF along rows: out_row = C . in_row with C = ifft diag(s) fft,
 // s = sinc(fftfreq(N) * os) real and even, so C is real.  Two real rows a, b
 // ride one complex transform z = a + i b: fft, times s, inverse fft gives
 // C a + i C b.  One block per row pair, one N-point buffer (the spectrum is
-// bit-reversed in place between the two transforms).
+// bit-reversed in place between the two transforms).  The float64 rows enter
+// and leave as double-float pairs by integer conversions (split_double,
+// widen_float), so the FP64 pipe only adds each output's two halves.
 __global__ void __launch_bounds__(512) pixel_filter_rows_kernel(const double* __restrict__ in,
                                                                 double* __restrict__ out, int N,
                                                                 int logN,
-                                                                const double2* __restrict__ tw,
+                                                                const float4* __restrict__ tw,
                                                                 const double* __restrict__ sinc) {
-  extern __shared__ double2 sm[];
+  extern __shared__ float4 smf[];
   const size_t r0 = 2 * (size_t)blockIdx.x;
   const double* ra = in + r0 * N;
   const double* rb = ra + N;
   const int shift = 32 - logN;
-  for (int i = threadIdx.x; i < N; i += blockDim.x)
-    sm[__brev((unsigned)i) >> shift] = make_double2(ra[i], rb[i]);
-  __syncthreads();
-  fft_stages(sm, N, logN, tw, 0);
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    const double k = sinc[i];
-    sm[i] = make_double2(sm[i].x * k, sm[i].y * k);
+    const float2 a = split_double(ra[i]), b = split_double(rb[i]);
+    smf[__brev((unsigned)i) >> shift] = make_float4(a.x, a.y, b.x, b.y);
+  }
+  __syncthreads();
+  fft_stages_df(smf, N, logN, tw, false);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const float2 k2 = split_double(sinc[i]);
+    const dfl k{k2.x, k2.y};
+    const float4 z = smf[i];
+    smf[i] = df_pack(df_mul({z.x, z.y}, k), df_mul({z.z, z.w}, k));
   }
   __syncthreads();
   for (int i = threadIdx.x; i < N; i += blockDim.x) {     // bit-reverse in place
     const int j = (int)(__brev((unsigned)i) >> shift);
     if (i < j) {
-      const double2 t = sm[i];
-      sm[i] = sm[j];
-      sm[j] = t;
+      const float4 t = smf[i];
+      smf[i] = smf[j];
+      smf[j] = t;
     }
   }
   __syncthreads();
-  fft_stages(sm, N, logN, tw, 1);
-  const double sc = 1.0 / N;
+  fft_stages_df(smf, N, logN, tw, true);
+  const float sc = 1.f / (float)N;                        // a power of two: exact
   double* oa = out + r0 * N;
   double* ob = oa + N;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    oa[i] = sm[i].x * sc;
-    ob[i] = sm[i].y * sc;
+    const float4 z = smf[i];
+    oa[i] = widen_float(z.x * sc) + widen_float(z.y * sc);
+    ob[i] = widen_float(z.z * sc) + widen_float(z.w * sc);
   }
 }
 
@@ -504,16 +580,17 @@ static int run_pixel(const double* img, int N, int os, void* ws, cudaStream_t s,
     // N x N intermediates
     double* R = reinterpret_cast<double*>(w->X);
     double* RT = reinterpret_cast<double*>(w->Y);
-    twiddle_kernel<<<cdiv(std::max(N / 2, 1), 256), 256, 0, s>>>(N, w->tw);
-    const size_t smem = (size_t)N * sizeof(double2);
+    float4* const twd = reinterpret_cast<float4*>(w->tw);   // N/2 entries of 16 bytes
+    twiddle_df_kernel<<<cdiv(std::max(N / 2, 1), 256), 256, 0, s>>>(N, twd);
+    const size_t smem = (size_t)N * sizeof(float4);
     LGB_CUDA(cudaFuncSetAttribute(pixel_filter_rows_kernel,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  8192 * (int)sizeof(double2)));
+                                  8192 * (int)sizeof(float4)));
     const int threads = std::min(512, std::max(32, N / 2));
     const dim3 tgrid(cdiv(N, 32), cdiv(N, 32)), tblock(32, 8);
-    pixel_filter_rows_kernel<<<N / 2, threads, smem, s>>>(img, R, N, logN, w->tw, w->sinc);
+    pixel_filter_rows_kernel<<<N / 2, threads, smem, s>>>(img, R, N, logN, twd, w->sinc);
     transpose_f64_kernel<<<tgrid, tblock, 0, s>>>(R, RT, N);
-    pixel_filter_rows_kernel<<<N / 2, threads, smem, s>>>(RT, R, N, logN, w->tw, w->sinc);
+    pixel_filter_rows_kernel<<<N / 2, threads, smem, s>>>(RT, R, N, logN, twd, w->sinc);
     transpose_f64_kernel<<<tgrid, tblock, 0, s>>>(R, RT, N);
     LGB_CUDA(cudaGetLastError());
     w->P = RT;
