@@ -16,7 +16,9 @@ tilts is one dense field.  Pupils whose segments carry their own tilts are
 propagated field by field through ``propagate_dft`` (same kernels, one
 launch sequence per field) and overlap-added on the device.
 """
+import concurrent.futures
 import ctypes
+import os
 import threading
 
 import numpy as np
@@ -231,6 +233,49 @@ class PSFPlan:
         return out
 
 
+_HOST_POOL = None
+_HOST_POOL_LOCK = threading.Lock()
+_HOST_WORKERS = max(1, min(8, os.cpu_count() or 1))
+_HOST_PARALLEL_MIN = 1 << 22          # elements below which one thread is faster
+
+
+def _host_pool():
+    global _HOST_POOL
+    with _HOST_POOL_LOCK:
+        if _HOST_POOL is None:
+            _HOST_POOL = concurrent.futures.ThreadPoolExecutor(max_workers=_HOST_WORKERS,
+                                                               thread_name_prefix='lgb-host')
+        return _HOST_POOL
+
+
+def _by_rows(fn, rows, size):
+    """fn(r0, r1) over blocks of rows in the host pool (numpy releases the GIL
+    in its loops, so the blocks run in parallel), or in one call when the
+    array is small."""
+    parts = min(_HOST_WORKERS, rows) if size >= _HOST_PARALLEL_MIN else 1
+    if parts <= 1:
+        fn(0, rows)
+        return
+    edges = np.linspace(0, rows, parts + 1).round().astype(int)
+    list(_host_pool().map(lambda k: fn(edges[k], edges[k + 1]), range(parts)))
+
+
+def _summed_mask(mask):
+    """mask.sum(axis=0) of an (S, H, W) mask by row blocks: each pixel adds
+    its S values in the same order, so the result is the same array."""
+    out = np.empty(mask.shape[1:], dtype=np.add.reduce(mask[:, :1, :1], axis=0).dtype)
+    _by_rows(lambda r0, r1: np.sum(mask[:, r0:r1], axis=0, out=out[r0:r1]), mask.shape[1],
+             mask.size)
+    return out
+
+
+def _product(a, b):
+    out = np.empty(np.broadcast_shapes(a.shape, b.shape), dtype=np.result_type(a, b))
+    _by_rows(lambda r0, r1: np.multiply(a[r0:r1], b[r0:r1], out=out[r0:r1]), out.shape[0],
+             out.size)
+    return out
+
+
 def dense_field(pupil):
     """Merged single field of a pupil without per-segment tilts: the slice
     covering every segment and amp*sum(masks) over it (lentil/plane.py:494-514
@@ -242,14 +287,15 @@ def dense_field(pupil):
     mask = np.asarray(dv.to_host(mask) if dv.is_tensor(mask) else mask, dtype=float)
     if amp.ndim != 2:
         raise NotImplementedError('broadband plan needs an amplitude array')
-    gmask = mask if mask.ndim == 2 else mask.sum(axis=0)
+    gmask = mask if mask.ndim == 2 else _summed_mask(mask)
     # the union of the segments' bounding boxes: segment masks are
     # transmissions (>= 0), so a pixel lies in some segment exactly where
     # their sum is positive -- one scan of the summed mask instead of one
     # per segment
     s = util.boundary_slice(gmask)
     opd_full = np.broadcast_to(opd, amp.shape) if opd.size == 1 else opd
-    return s, amp * gmask, np.ascontiguousarray(opd_full, dtype=float)
+    amp_eff = _product(amp, gmask) if amp.shape == gmask.shape else amp * gmask
+    return s, amp_eff, np.ascontiguousarray(opd_full, dtype=float)
 
 
 def _device_field(pupil):
