@@ -72,6 +72,12 @@ class _PlaneBase:
             return (a != 0) if dv.is_tensor(a) else np.copy(a).astype(bool)
         return self._mask
 
+    def _mask_is_amplitude(self):
+        """True when the mask is the amplitude's nonzero pattern: no mask was
+        given and ``__mask__`` is not overridden.  Its shape and rank are then
+        the amplitude's, and amplitude * mask is the amplitude itself."""
+        return self._mask is None and type(self).__mask__ is _PlaneBase.__mask__
+
     def __opd__(self):
         return self._opd
 
@@ -130,17 +136,21 @@ class _PlaneBase:
         rmin, rmax, cmin, cmax = util.boundary(_np(self.global_mask))
         return np.max(np.max((rmax - rmin, cmax - cmin)) * np.asarray(self.pixelscale))
 
+    def _mask_meta(self):
+        """(shape, rank) of the mask, without building an amplitude-derived one."""
+        m = self.amplitude if self._mask_is_amplitude() else self.mask
+        shp = tuple(m.shape) if hasattr(m, 'shape') else np.shape(m)
+        return shp, len(shp)
+
     @property
     def shape(self):
-        m = self.mask
-        shp = tuple(m.shape) if hasattr(m, 'shape') else np.shape(m)
-        return shp if self.size == 1 else shp[1:]
+        shp, nd = self._mask_meta()
+        return shp if nd in (0, 1, 2) else shp[1:]
 
     @property
     def size(self):
-        m = self.mask
-        nd = m.dim() if dv.is_tensor(m) else np.ndim(m)
-        return 1 if nd in (0, 1, 2) else int(m.shape[0])
+        shp, nd = self._mask_meta()
+        return 1 if nd in (0, 1, 2) else int(shp[0])
 
     @property
     def frozen(self):
@@ -209,9 +219,12 @@ class Plane(_PlaneBase):
         opd_d = dv.to_device(opd, torch.float64) if opd_arr else None
         amp_v = 0.0 if amp_arr else _scalar(amp)
         opd_v = 0.0 if opd_arr else _scalar(opd)
-        mask_d = dv.to_device(mask, torch.float64) if amp_arr else None
+        # an amplitude-derived mask multiplies the amplitude by one where it
+        # is nonzero and by zero where it is zero: nothing to apply
+        mask_d = dv.to_device(mask, torch.float64) if amp_arr and not self._mask_is_amplitude() \
+            else None
         plane_shape = tuple(self.shape)
-        slices = self._slice
+        slices = _plane_slice(mask)
         for f in wavefront.data:
             for n, s in enumerate(slices):
                 phasor = self._phasor(n, s, amp_d, amp_v, opd_d, opd_v, mask_d, plane_shape,
