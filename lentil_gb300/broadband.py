@@ -248,6 +248,16 @@ def _host_pool():
         return _HOST_POOL
 
 
+def _forget_host_pool():
+    # a forked child inherits the pool object but not its threads
+    global _HOST_POOL, _HOST_POOL_LOCK
+    _HOST_POOL, _HOST_POOL_LOCK = None, threading.Lock()
+
+
+if hasattr(os, 'register_at_fork'):
+    os.register_at_fork(after_in_child=_forget_host_pool)
+
+
 def _by_rows(fn, rows, size):
     """fn(r0, r1) over blocks of rows in the host pool (numpy releases the GIL
     in its loops, so the blocks run in parallel), or in one call when the

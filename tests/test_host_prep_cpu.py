@@ -2,6 +2,7 @@
 row-block parallel mask sum and amplitude product equal numpy's own
 (lentil/plane.py:494-514 summed over segments)."""
 import numpy as np
+import pytest
 
 from lentil_gb300 import broadband, shapes, util
 
@@ -31,3 +32,20 @@ def test_dense_field_matches_numpy():
     assert s == util.boundary_slice(g)
     assert np.array_equal(amp_eff, amp * g)
     assert np.array_equal(o, opd)
+
+
+@pytest.mark.filterwarnings('ignore:This process .* is multi-threaded:DeprecationWarning')
+def test_host_pool_after_fork():
+    # a child forked after the pool started gets a fresh pool, not dead threads
+    import multiprocessing as mp
+    segs = _segments(1024)
+    broadband._summed_mask(segs)                      # the parent's pool is running
+    ctx = mp.get_context('fork')
+    with ctx.Pool(1) as pool:
+        ok = pool.apply(_child_sum_ok, ())
+    assert ok
+
+
+def _child_sum_ok():
+    segs = _segments(1024)
+    return bool(np.array_equal(broadband._summed_mask(segs), segs.sum(axis=0)))
