@@ -193,6 +193,37 @@ def test_plan_batch_matches_single(cuda_device):
             assert lo.peak_normalised_error(outb[b], o1[0]) < tol
 
 
+def test_execute_streams_matches_execute(cuda_device):
+    # PSFs alternating over two streams with a workspace each equal the same
+    # PSFs executed one by one on the caller's stream
+    rng = np.random.default_rng(15)
+    H = 96
+    amp = lo.normalize_power(lg.circle((H, H), 44))
+    wl = np.linspace(500e-9, 800e-9, 20)
+    alphas = [((1 / 88) * 5e-6 / (l * 10 * 2),) * 2 for l in wl]
+    shifts = [(0.0, 0.0)] * len(wl)
+    n = 5
+    O = torch.as_tensor(np.stack([lg.zernike_compose(amp, np.r_[0, rng.normal(0, 30e-9, 10)])
+                                  for _ in range(n)]), device='cuda')
+    A1 = torch.as_tensor(amp[None].copy(), device='cuda')
+    An = torch.as_tensor(np.stack([amp * rng.uniform(0.5, 1.5) for _ in range(n)]), device='cuda')
+    W1 = torch.as_tensor(rng.uniform(0.5, 1.5, (1, len(wl))), device='cuda')
+    Wn = torch.as_tensor(rng.uniform(0.5, 1.5, (n, len(wl))), device='cuda')
+    for prec in ('split-bf16', 'fp64'):
+        plan = lg.PSFPlan((H, H), (0, 0, H, H), (0, 0), wl, alphas, shifts, (80, 72), (80, 72),
+                          (0, 0), batch=1, precision=prec)
+        for A, W in ((A1, W1), (An, Wn)):
+            one = torch.stack([plan.execute(A if A.shape[0] == 1 else A[k:k + 1], O[k:k + 1],
+                                            W if W.shape[0] == 1 else W[k:k + 1])[0]
+                               for k in range(n)])
+            out = torch.full((n, 80, 72), 7.0, dtype=torch.float64, device='cuda')
+            got = plan.execute_streams(A, O, W, out)
+            assert got is out
+            plan.stream_status()
+            tol = (1e-13 if prec == 'fp64' else 1e-6) * float(one.abs().max())
+            assert float((out - one).abs().max()) <= tol, prec
+
+
 def test_broadband_many_wavelengths(cuda_device):
     # 520 wavelengths: the phasor operand kernel's blocks then take more than
     # 32 wavelengths each (16 groups at most), so they reload their
