@@ -1,16 +1,19 @@
 """Benchmark: polychromatic 1024^2 PSFs/s of the broadband segmented workload.
 
-Workload (one "step" = one batch of PSFs through the fused broadband plan):
-1024x1024 pupil of 18 hexagonal segments (two rings, empty centre, 2 px
-gaps), per-segment piston/tip/tilt ~ N(0, 50 nm), global Noll 2-22 ~
-N(0, 15 nm), 64 wavelengths over 500-900 nm weighted by a 5800 K blackbody,
-512x512 detector at oversample 2 (1024^2 field per wavelength).  Inputs are
-seeded synthetic arrays of those shapes.
+Workload (one "step" = 32 PSFs through the fused broadband plan, each with
+its own OPD map): 1024x1024 pupil of 18 hexagonal segments (two rings, empty
+centre, 2 px gaps), per-segment piston/tip/tilt ~ N(0, 50 nm), global Noll
+2-22 ~ N(0, 15 nm), 64 wavelengths over 500-900 nm weighted by a 5800 K
+blackbody, 512x512 detector at oversample 2 (1024^2 field per wavelength).
+Inputs are seeded synthetic arrays of those shapes.  The timed region runs a
+step's PSFs over two streams (PSFPlan.execute_streams); per-kernel times for
+the rooflines come from the same steps run serially right after it.
 
 Arms:
   default           the split-precision tensor-core plan (lentil_gb300) on cuda
-  --impl reference  lentil's own CPU algorithm (the numpy restatement under
-                    oracle/) on the host cores, bounded sample of wavelengths
+  --impl reference  lentil 0.8.8 itself (installed under baseline/_ref; else
+                    the numpy restatement under oracle/) on the host cores,
+                    a bounded sample of wavelengths per step
 
 Prints ONE JSON line (rank 0).  Under torchrun every rank runs an independent
 replica on its own GPU (the path has no data exchange); value is the total
