@@ -186,11 +186,11 @@ class PSFPlan:
             raise ValueError(f'out must hold {count} images')
         pick = lambda t, k: t if t.shape[0] == 1 else t[k:k + 1]
         cur = torch.cuda.current_stream()
-        if (count == 1 or torch.cuda.is_current_stream_capturing()
-                or _lib.precision_code(self.precision) == _lib.FP64):
-            for k in range(count):
+        capturing = torch.cuda.is_current_stream_capturing()
+        if count == 1 or capturing or _lib.precision_code(self.precision) == _lib.FP64:
+            for k in range(count):        # (no status wait inside a capture)
                 self.execute(pick(amp, k), opd[k:k + 1], pick(weights, k), out=out[k:k + 1],
-                             check=check)
+                             check=check and not capturing)
             return out
         if self._lanes is None:
             nbytes = max(1, self.workspace_bytes(1))

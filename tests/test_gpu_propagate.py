@@ -222,6 +222,28 @@ def test_execute_streams_matches_execute(cuda_device):
             plan.stream_status()
             tol = (1e-13 if prec == 'fp64' else 1e-6) * float(one.abs().max())
             assert float((out - one).abs().max()) <= tol, prec
+        # one PSF, and inside a CUDA-graph capture: in order on the caller's stream
+        out1 = plan.execute_streams(A1, O[:1], W1, torch.empty((1, 80, 72), dtype=torch.float64,
+                                                               device='cuda'))
+        ref1 = plan.execute(A1, O[:1], W1)
+        assert float((out1 - ref1).abs().max()) <= 1e-6 * float(ref1.abs().max())
+        if prec != 'fp64':
+            outg = torch.empty((n, 80, 72), dtype=torch.float64, device='cuda')
+            plan.execute_streams(A1, O, W1, outg)            # warm: plan memory, tuner decided
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                g.capture_begin(capture_error_mode='thread_local')
+                plan.execute_streams(A1, O, W1, outg)
+                g.capture_end()
+            torch.cuda.current_stream().wait_stream(side)
+            outg.zero_()
+            g.replay()
+            torch.cuda.synchronize()
+            ref = plan.execute_streams(A1, O, W1, torch.empty_like(outg))
+            assert float((outg - ref).abs().max()) <= 1e-6 * float(ref.abs().max())
 
 
 def test_broadband_many_wavelengths(cuda_device):
