@@ -299,6 +299,16 @@ int lgb_basis_expand(const float* basis, const double* coeffs, int K, size_t P, 
 size_t lgb_basis_project_workspace_size(int K);
 int lgb_basis_project(const float* basis, const double* grad, int K, size_t P, double* out,
                       void* workspace, size_t workspace_bytes, lgb_stream stream);
+/* Squared-error loss of phase retrieval: *loss = sum_p (I[p] - T[p])^2
+ * (FP64, fixed-order reduction, written on the device; workspace
+ * lgb_sq_error_workspace_size() bytes) and its gradient dI[p] =
+ * 2 (I[p] - T[p]) * (*dL) with dL a device scalar (n == 0: *loss = 0, and
+ * I, T, dI may be null). */
+size_t lgb_sq_error_workspace_size(void);
+int lgb_sq_error(const double* I, const double* T, size_t n, double* loss, void* workspace,
+                 size_t workspace_bytes, lgb_stream stream);
+int lgb_sq_error_grad(const double* I, const double* T, size_t n, const double* dL, double* dI,
+                      lgb_stream stream);
 /* K phasors amp * exp(2 pi i opd[k] / wavelength) over the slice (r0, c0,
  * m, n) of H x W planes, out[K][m][n], in one launch.  fast != 0 evaluates
  * the phase in float-float and the sine in FP32 (about 1e-7 relative, for

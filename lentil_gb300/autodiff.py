@@ -136,6 +136,40 @@ class _BasisOPD(torch.autograd.Function):
         return out, None
 
 
+class _SquaredError(torch.autograd.Function):
+    """sum (I - T)^2 and its gradient 2 (I - T) dL in one kernel pass each
+    (lgb_sq_error, lgb_sq_error_grad), in place of a chain of FP64
+    elementwise kernels and reductions."""
+
+    @staticmethod
+    def forward(ctx, I, T):
+        if I.shape != T.shape:
+            raise ValueError(f'images {tuple(I.shape)} and targets {tuple(T.shape)} differ')
+        I = I.to(torch.float64).contiguous()
+        T = T.to(torch.float64).contiguous()
+        loss = torch.empty((), dtype=torch.float64, device=I.device)
+        ws = torch.empty(_lib.load().lgb_sq_error_workspace_size(), dtype=torch.uint8,
+                         device=I.device)
+        _lib.call('lgb_sq_error', I.data_ptr(), T.data_ptr(), I.numel(), loss.data_ptr(),
+                  ws.data_ptr(), ws.numel(), dv.stream_ptr())
+        ctx.save_for_backward(I, T)
+        return loss
+
+    @staticmethod
+    def backward(ctx, grad):
+        I, T = ctx.saved_tensors
+        g = grad.to(torch.float64).contiguous()
+        dI = torch.empty_like(I)
+        _lib.call('lgb_sq_error_grad', I.data_ptr(), T.data_ptr(), I.numel(), g.data_ptr(),
+                  dI.data_ptr(), dv.stream_ptr())
+        return dI, (-dI if ctx.needs_input_grad[1] else None)
+
+
+def squared_error(I, T):
+    """sum((I - T) ** 2) as one device pass, differentiable in I and T."""
+    return _SquaredError.apply(I, T)
+
+
 class PhaseRetrieval:
     """Focus-diverse phase-retrieval loss sum_k sum (PSF_k - target_k)^2 over
     OPD = basis . coeffs (+ an optional free-form map), with the diversity
@@ -174,7 +208,7 @@ class PhaseRetrieval:
     def loss(self, coeffs, free=None):
         o = self.opd(coeffs, free)
         stack = o.unsqueeze(0) + torch.stack(self.diversity)   # all images in one batched MFT
-        return ((mft_intensity(stack, self.amp, self.g) - torch.stack(self.targets)) ** 2).sum()
+        return squared_error(mft_intensity(stack, self.amp, self.g), torch.stack(self.targets))
 
     def graphed_loss(self, coeffs):
         """``loss(coeffs)`` replayed from CUDA graphs (captured on first use)."""
@@ -184,7 +218,7 @@ class PhaseRetrieval:
 
             def fn(c):
                 o = self.opd(c)
-                return ((mft_intensity(o.unsqueeze(0) + div, self.amp, self.g) - tgt) ** 2).sum()
+                return squared_error(mft_intensity(o.unsqueeze(0) + div, self.amp, self.g), tgt)
 
             sample = coeffs.detach().clone().requires_grad_(True)
             with fourier.pinned_plans() as pins:

@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(256) basis_expand_kernel(const float* __restri
       }
     }
     for (; k < K; ++k) a0 = fmaf(cs[k], __ldg(B + (size_t)k * P + p), a0);
-    out[p] = (double)(a0 + a1);
+    out[p] = widen_float(a0 + a1);                 // integer widening: no FP64 pipe
   }
 }
 
@@ -56,13 +56,16 @@ __global__ void __launch_bounds__(256) basis_project_partial_kernel(const float*
   const int k0 = blockIdx.y * PROJ_KG, nk = min(PROJ_KG, K - k0);
   const size_t per = (P + gridDim.x - 1) / gridDim.x;
   const size_t p0 = (size_t)blockIdx.x * per, p1 = min(P, p0 + per);
-  // a thread sums only a few pixels (P / gridDim.x / blockDim.x): FP32 there,
-  // FP64 from the warp reduction on (this part's FP64 adds are as slow as FMAs)
+  // a thread sums only a few pixels (P / gridDim.x / blockDim.x), and a warp
+  // 32 such sums: FP32 up to there, FP64 for the block's warps and the blocks
+  // (this part's FP64 pipe retires about two operations a clock per SM, so
+  // an FP64 shuffle reduction of every warp's sums took most of the time);
+  // the gradient enters as a truncated float by integer operations
   float acc[PROJ_KG];
 #pragma unroll
   for (int j = 0; j < PROJ_KG; ++j) acc[j] = 0.f;
   for (size_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    const float gv = (float)g[p];
+    const float gv = truncate_double(g[p]);
 #pragma unroll
     for (int j = 0; j < PROJ_KG; ++j)
       if (j < nk) acc[j] = fmaf(__ldg(B + (size_t)(k0 + j) * P + p), gv, acc[j]);
@@ -70,10 +73,10 @@ __global__ void __launch_bounds__(256) basis_project_partial_kernel(const float*
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
   for (int j = 0; j < PROJ_KG; ++j) {
-    double v = (double)acc[j];
+    float v = acc[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[w][j] = v;
+    if (lane == 0) red[w][j] = widen_float(v);
   }
   __syncthreads();
   if (threadIdx.x < nk) {
@@ -92,9 +95,81 @@ __global__ void basis_project_final_kernel(const double* __restrict__ partial, i
   out[k] = t;
 }
 
+// Squared-error loss L = sum (I - T)^2 and its gradient dL/dI = 2 (I - T) dL
+// (the phase-retrieval loss), each one pass over the images, FP64: the
+// per-thread sums and the fixed-order block reduction make L deterministic.
+constexpr int SQE_BLOCKS = 152;
+
+__global__ void __launch_bounds__(256) sq_error_partial_kernel(const double* __restrict__ I,
+                                                               const double* __restrict__ T,
+                                                               size_t n,
+                                                               double* __restrict__ partial) {
+  __shared__ double red[8];
+  double acc = 0.0;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const double d = I[p] - T[p];
+    acc = fma(d, d, acc);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void sq_error_final_kernel(const double* __restrict__ partial, int nblocks,
+                                      double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double t = 0.0;
+  for (int b = 0; b < nblocks; ++b) t += partial[b];
+  *out = t;
+}
+
+__global__ void sq_error_grad_kernel(const double* __restrict__ I, const double* __restrict__ T,
+                                     size_t n, const double* __restrict__ dL,
+                                     double* __restrict__ dI) {
+  const double s = 2.0 * *dL;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += (size_t)gridDim.x * blockDim.x)
+    dI[p] = s * (I[p] - T[p]);
+}
+
 }  // namespace lgb
 
 using namespace lgb;
+
+extern "C" size_t lgb_sq_error_workspace_size(void) { return SQE_BLOCKS * sizeof(double); }
+
+extern "C" int lgb_sq_error(const double* I, const double* T, size_t n, double* loss,
+                            void* workspace, size_t workspace_bytes, lgb_stream stream) {
+  LGB_RANGE("lgb_sq_error");
+  LGB_REQUIRE(((I && T) || n == 0) && loss && workspace, LGB_EINVAL, "sq_error: null pointer");
+  LGB_REQUIRE(workspace_bytes >= lgb_sq_error_workspace_size(), LGB_EWORKSPACE,
+              "sq_error: workspace too small");
+  cudaStream_t s = as_stream(stream);
+  double* partial = static_cast<double*>(workspace);
+  const int blocks = (int)std::max<size_t>(1, std::min<size_t>(SQE_BLOCKS, (n + 255) / 256));
+  sq_error_partial_kernel<<<blocks, 256, 0, s>>>(I, T, n, partial);
+  sq_error_final_kernel<<<1, 32, 0, s>>>(partial, blocks, loss);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
+
+extern "C" int lgb_sq_error_grad(const double* I, const double* T, size_t n, const double* dL,
+                                 double* dI, lgb_stream stream) {
+  LGB_RANGE("lgb_sq_error_grad");
+  if (n == 0) return LGB_OK;
+  LGB_REQUIRE(I && T && dL && dI, LGB_EINVAL, "sq_error_grad: null pointer");
+  const int blocks = (int)std::max<size_t>(1, std::min<size_t>((size_t)8 * sm_count(), (n + 255) / 256));
+  sq_error_grad_kernel<<<blocks, 256, 0, as_stream(stream)>>>(I, T, n, dL, dI);
+  LGB_CUDA(cudaGetLastError());
+  return LGB_OK;
+}
 
 extern "C" int lgb_basis_expand(const float* basis, const double* coeffs, int K, size_t P,
                                 double* out, lgb_stream stream) {

@@ -249,3 +249,20 @@ def test_basis_expand_and_project(cuda_device):
         assert torch.equal(res[0], res[1])
         refp = torch.einsum('khw,hw->k', B.double(), g)
         assert (res[0] - refp).abs().max().item() < 1e-5 * refp.abs().max().item() + 1e-12
+
+
+def test_squared_error_matches_torch(cuda_device):
+    # the fused loss kernel and its gradient against torch's own expression
+    g = torch.Generator(device='cuda').manual_seed(5)
+    for shape in ((3, 64, 64), (1000,), (0,), (2, 1, 7)):
+        I = torch.rand(shape, dtype=torch.float64, device='cuda', generator=g).requires_grad_(True)
+        T = torch.rand(shape, dtype=torch.float64, device='cuda', generator=g).requires_grad_(True)
+        L = autodiff.squared_error(I, T)
+        L.backward(torch.tensor(1.7, dtype=torch.float64, device='cuda'))
+        gI, gT = I.grad.clone(), T.grad.clone()
+        I.grad = T.grad = None
+        R = ((I - T) ** 2).sum()
+        R.backward(torch.tensor(1.7, dtype=torch.float64, device='cuda'))
+        assert abs(L.item() - R.item()) <= 1e-13 * max(1.0, abs(R.item()))
+        assert torch.allclose(gI, I.grad, rtol=1e-15, atol=0)
+        assert torch.allclose(gT, T.grad, rtol=1e-15, atol=0)
