@@ -86,48 +86,68 @@ __global__ void __launch_bounds__(256) basis_project_partial_kernel(const float*
   }
 }
 
+// FP64 sum of n values in a fixed order by one warp: lane l adds values
+// l, l+32, ..., then a shuffle tree (this part's FP64 adds have a long
+// latency: a single thread walking 152 partials took ~14 us)
+__device__ __forceinline__ double warp_sum_fixed(const double* __restrict__ v, int n) {
+  const int lane = threadIdx.x & 31;
+  double t = 0.0;
+  for (int i = lane; i < n; i += 32) t += v[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  return t;
+}
+
+// out[k] = sum of mode k's partials: one warp per mode
 __global__ void basis_project_final_kernel(const double* __restrict__ partial, int nblocks, int K,
                                            double* __restrict__ out) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= K) return;
-  double t = 0.0;
-  for (int b = 0; b < nblocks; ++b) t += partial[(size_t)k * nblocks + b];
-  out[k] = t;
+  const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (k >= K) return;                                   // (warp-uniform)
+  const double t = warp_sum_fixed(partial + (size_t)k * nblocks, nblocks);
+  if ((threadIdx.x & 31) == 0) out[k] = t;
 }
 
 // Squared-error loss L = sum (I - T)^2 and its gradient dL/dI = 2 (I - T) dL
 // (the phase-retrieval loss), each one pass over the images, FP64: the
-// per-thread sums and the fixed-order block reduction make L deterministic.
-constexpr int SQE_BLOCKS = 152;
+// per-thread sums and the fixed-order block reductions make L
+// deterministic.  Enough blocks that each thread keeps only a few dependent
+// FP64 operations in flight.
+constexpr int SQE_MAX_BLOCKS = 2048;
 
 __global__ void __launch_bounds__(256) sq_error_partial_kernel(const double* __restrict__ I,
                                                                const double* __restrict__ T,
                                                                size_t n,
                                                                double* __restrict__ partial) {
   __shared__ double red[8];
-  double acc = 0.0;
-  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
-       p += (size_t)gridDim.x * blockDim.x) {
-    const double d = I[p] - T[p];
-    acc = fma(d, d, acc);
+  double a0 = 0.0, a1 = 0.0;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p + stride < n; p += 2 * stride) {              // two independent chains
+    const double d0 = I[p] - T[p], d1 = I[p + stride] - T[p + stride];
+    a0 = fma(d0, d0, a0);
+    a1 = fma(d1, d1, a1);
   }
+  if (p < n) {
+    const double d = I[p] - T[p];
+    a0 = fma(d, d, a0);
+  }
+  double acc = a0 + a1;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-    partial[blockIdx.x] = t;
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
   }
 }
 
 __global__ void sq_error_final_kernel(const double* __restrict__ partial, int nblocks,
                                       double* __restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double t = 0.0;
-  for (int b = 0; b < nblocks; ++b) t += partial[b];
-  *out = t;
+  const double t = warp_sum_fixed(partial, nblocks);    // one warp
+  if (threadIdx.x == 0) *out = t;
 }
 
 __global__ void sq_error_grad_kernel(const double* __restrict__ I, const double* __restrict__ T,
@@ -143,7 +163,7 @@ __global__ void sq_error_grad_kernel(const double* __restrict__ I, const double*
 
 using namespace lgb;
 
-extern "C" size_t lgb_sq_error_workspace_size(void) { return SQE_BLOCKS * sizeof(double); }
+extern "C" size_t lgb_sq_error_workspace_size(void) { return SQE_MAX_BLOCKS * sizeof(double); }
 
 extern "C" int lgb_sq_error(const double* I, const double* T, size_t n, double* loss,
                             void* workspace, size_t workspace_bytes, lgb_stream stream) {
@@ -153,7 +173,8 @@ extern "C" int lgb_sq_error(const double* I, const double* T, size_t n, double* 
               "sq_error: workspace too small");
   cudaStream_t s = as_stream(stream);
   double* partial = static_cast<double*>(workspace);
-  const int blocks = (int)std::max<size_t>(1, std::min<size_t>(SQE_BLOCKS, (n + 255) / 256));
+  const int blocks = (int)std::max<size_t>(
+      1, std::min<size_t>({(size_t)SQE_MAX_BLOCKS, (size_t)8 * sm_count(), (n + 1023) / 1024}));
   sq_error_partial_kernel<<<blocks, 256, 0, s>>>(I, T, n, partial);
   sq_error_final_kernel<<<1, 32, 0, s>>>(partial, blocks, loss);
   LGB_CUDA(cudaGetLastError());
@@ -199,7 +220,7 @@ extern "C" int lgb_basis_project(const float* basis, const double* grad, int K, 
   cudaStream_t s = as_stream(stream);
   basis_project_partial_kernel<<<dim3(PROJ_BLOCKS, cdiv(K, PROJ_KG)), 256, 0, s>>>(basis, grad, K,
                                                                                    P, partial);
-  basis_project_final_kernel<<<cdiv(K, 128), 128, 0, s>>>(partial, PROJ_BLOCKS, K, out);
+  basis_project_final_kernel<<<cdiv(K, 4), 128, 0, s>>>(partial, PROJ_BLOCKS, K, out);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
 }
