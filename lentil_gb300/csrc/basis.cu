@@ -14,7 +14,7 @@
 namespace lgb {
 
 constexpr int BASIS_MAX_K = 1024;
-constexpr int PROJ_BLOCKS = 152;
+constexpr int PROJ_BLOCKS = 76;
 
 // out[p] = sum_k c[k] B[k][p]; c staged in shared memory as FP32
 __global__ void __launch_bounds__(256) basis_expand_kernel(const float* __restrict__ B,
@@ -79,10 +79,14 @@ __global__ void __launch_bounds__(256) basis_project_partial_kernel(const float*
     if (lane == 0) red[w][j] = widen_float(v);
   }
   __syncthreads();
-  if (threadIdx.x < nk) {
-    double t = 0.0;
-    for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww) t += red[ww][threadIdx.x];
-    partial[(size_t)(k0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  // the block's 8 warp sums of mode j: threads 8j .. 8j+7, a 3-level
+  // shuffle tree in a fixed order
+  if (threadIdx.x < 8 * PROJ_KG) {
+    const int j = threadIdx.x >> 3, ww = threadIdx.x & 7;
+    double t = red[ww][j];
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (ww == 0 && j < nk) partial[(size_t)(k0 + j) * gridDim.x + blockIdx.x] = t;
   }
 }
 
