@@ -34,55 +34,11 @@ __device__ __forceinline__ double sinc_os(int k, int N, double os) {
 }
 
 // ---------------------------------------------------------------- FFT path
-__global__ void twiddle_kernel(int N, double2* __restrict__ tw) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= N / 2) return;
-  double s, c;
-  sincospi(-2.0 * (double)k / N, &s, &c);                 // exp(-2 pi i k / N)
-  tw[k] = make_double2(c, s);
-}
-
 __global__ void real_to_complex_kernel(const double* __restrict__ x, double2* __restrict__ z,
                                        size_t count) {
   for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < count;
        p += (size_t)gridDim.x * blockDim.x)
     z[p] = make_double2(x[p], 0.0);
-}
-
-// Radix-2 butterflies over a bit-reversed row in shared memory: natural
-// order out (the caller syncs before; this returns after a final sync).
-__device__ __forceinline__ void fft_stages(double2* sm, int N, int logN,
-                                           const double2* __restrict__ tw, int inverse) {
-  for (int s = 1; s <= logN; ++s) {
-    const int half = 1 << (s - 1);
-    const int stride = N >> s;                         // twiddle index step
-    for (int b = threadIdx.x; b < N / 2; b += blockDim.x) {
-      const int pos = b & (half - 1);
-      const int i0 = ((b >> (s - 1)) << s) + pos, i1 = i0 + half;
-      double2 w = tw[pos * stride];
-      if (inverse) w.y = -w.y;
-      const double2 a = sm[i0], v = sm[i1];
-      const double2 t = make_double2(w.x * v.x - w.y * v.y, w.x * v.y + w.y * v.x);
-      sm[i0] = make_double2(a.x + t.x, a.y + t.y);
-      sm[i1] = make_double2(a.x - t.x, a.y - t.y);
-    }
-    __syncthreads();
-  }
-}
-
-// In-place FFT of every row (length N = 2^logN) in shared memory.
-__global__ void __launch_bounds__(512) fft_rows_kernel(double2* __restrict__ data, int N, int logN,
-                                                       const double2* __restrict__ tw,
-                                                       int inverse) {
-  extern __shared__ double2 sm[];
-  double2* row = data + (size_t)blockIdx.x * N;
-  for (int i = threadIdx.x; i < N; i += blockDim.x)
-    sm[__brev((unsigned)i) >> (32 - logN)] = row[i];
-  __syncthreads();
-  fft_stages(sm, N, logN, tw, inverse);
-  const double scale = inverse ? 1.0 / N : 1.0;
-  for (int i = threadIdx.x; i < N; i += blockDim.x)
-    row[i] = make_double2(sm[i].x * scale, sm[i].y * scale);
 }
 
 // Double-float arithmetic: a value as the unevaluated sum hi + lo of two
@@ -150,6 +106,30 @@ __device__ __forceinline__ void fft_stages_df(float4* sm, int N, int logN,
       sm[i1] = df_pack(df_sub(ar, tr), df_sub(ai, ti));
     }
     __syncthreads();
+  }
+}
+
+// In-place FFT of every complex float64 row (length N = 2^logN) in shared
+// memory, in double-float arithmetic (the power-spectrum filter); the
+// inverse scales by 1/N.
+__global__ void __launch_bounds__(512) fft_rows_kernel(double2* __restrict__ data, int N, int logN,
+                                                       const float4* __restrict__ tw,
+                                                       int inverse) {
+  extern __shared__ float4 smf[];
+  double2* row = data + (size_t)blockIdx.x * N;
+  const int shift = 32 - logN;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double2 v = row[i];
+    const float2 re = split_double(v.x), im = split_double(v.y);
+    smf[__brev((unsigned)i) >> shift] = make_float4(re.x, re.y, im.x, im.y);
+  }
+  __syncthreads();
+  fft_stages_df(smf, N, logN, tw, inverse != 0);
+  const float sc = inverse ? 1.f / (float)N : 1.f;      // a power of two: exact
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const float4 z = smf[i];
+    row[i] = make_double2(widen_float(z.x * sc) + widen_float(z.y * sc),
+                          widen_float(z.z * sc) + widen_float(z.w * sc));
   }
 }
 
@@ -833,19 +813,20 @@ extern "C" int lgb_power_spectrum(const double* noise, const double* mask, int N
   int logN;
   const double2* spatial;
   if (fft_size(N, &logN)) {
-    const size_t smem = (size_t)N * sizeof(double2);
+    const size_t smem = (size_t)N * sizeof(float4);
     LGB_CUDA(cudaFuncSetAttribute(fft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  8192 * (int)sizeof(double2)));
+                                  8192 * (int)sizeof(float4)));
     const int threads = std::min(512, std::max(32, N / 2));
     const dim3 tgrid(cdiv(N, 32), cdiv(N, 32)), tblock(32, 8);
-    twiddle_kernel<<<cdiv(std::max(N / 2, 1), 256), 256, 0, s>>>(N, w.tw);
-    fft_rows_kernel<<<N, threads, smem, s>>>(w.X, N, logN, w.tw, 0);
+    float4* const twd = reinterpret_cast<float4*>(w.tw);     // N/2 entries of 16 bytes
+    twiddle_df_kernel<<<cdiv(std::max(N / 2, 1), 256), 256, 0, s>>>(N, twd);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w.X, N, logN, twd, 0);
     transpose_c128_kernel<<<tgrid, tblock, 0, s>>>(w.X, w.Y, N);
-    fft_rows_kernel<<<N, threads, smem, s>>>(w.Y, N, logN, w.tw, 0);          // Y = fft2(X)^T
+    fft_rows_kernel<<<N, threads, smem, s>>>(w.Y, N, logN, twd, 0);           // Y = fft2(X)^T
     psd_filter_kernel<<<dim3(cdiv(N, 128), N), 128, 0, s>>>(w.Y, N, f0, exponent, w.sums);
-    fft_rows_kernel<<<N, threads, smem, s>>>(w.Y, N, logN, w.tw, 1);
+    fft_rows_kernel<<<N, threads, smem, s>>>(w.Y, N, logN, twd, 1);
     transpose_c128_kernel<<<tgrid, tblock, 0, s>>>(w.Y, w.X, N);
-    fft_rows_kernel<<<N, threads, smem, s>>>(w.X, N, logN, w.tw, 1);          // X = ifft2(...)
+    fft_rows_kernel<<<N, threads, smem, s>>>(w.X, N, logN, twd, 1);           // X = ifft2(...)
     LGB_CUDA(cudaGetLastError());
     spatial = w.X;
   } else {
