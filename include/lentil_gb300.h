@@ -299,6 +299,14 @@ int lgb_basis_expand(const float* basis, const double* coeffs, int K, size_t P, 
 size_t lgb_basis_project_workspace_size(int K);
 int lgb_basis_project(const float* basis, const double* grad, int K, size_t P, double* out,
                       void* workspace, size_t workspace_bytes, lgb_stream stream);
+/* The same over `count` planes at once (focus-diverse images):
+ * out[i][p] = sum_k coeffs[k] basis[k][p] + add[i][p] (add may be NULL), and
+ * out[k] = sum_p basis[k][p] sum_i grad[i][p]. */
+int lgb_basis_expand_stack(const float* basis, const double* coeffs, int K, size_t P,
+                           const double* add, int count, double* out, lgb_stream stream);
+int lgb_basis_project_stack(const float* basis, const double* grad, int count, int K, size_t P,
+                            double* out, void* workspace, size_t workspace_bytes,
+                            lgb_stream stream);
 /* Squared-error loss of phase retrieval: *loss = sum_p (I[p] - T[p])^2
  * (FP64, fixed-order reduction, written on the device; workspace
  * lgb_sq_error_workspace_size() bytes) and its gradient dI[p] =

@@ -80,6 +80,10 @@ SIGNATURES = {
     'lgb_basis_project_workspace_size': (c_size_t, [c_int]),
     'lgb_basis_project': (c_int, [c_void_p, c_void_p, c_int, c_size_t, c_void_p, c_void_p,
                                   c_size_t, c_void_p]),
+    'lgb_basis_expand_stack': (c_int, [c_void_p, c_void_p, c_int, c_size_t, c_void_p, c_int,
+                                       c_void_p, c_void_p]),
+    'lgb_basis_project_stack': (c_int, [c_void_p, c_void_p, c_int, c_int, c_size_t, c_void_p,
+                                        c_void_p, c_size_t, c_void_p]),
     'lgb_sq_error_workspace_size': (c_size_t, []),
     'lgb_sq_error': (c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p]),
     'lgb_sq_error_grad': (c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]),

@@ -136,6 +136,38 @@ class _BasisOPD(torch.autograd.Function):
         return out, None
 
 
+class _StackedOPD(torch.autograd.Function):
+    """OPD_i = sum_k c_k B_k + D_i for the diversity maps D [n, H, W] in one
+    pass over the FP32 basis, and dL/dc = B . sum_i dL/dOPD_i in one more
+    (lgb_basis_expand_stack / lgb_basis_project_stack), in place of a
+    broadcast add and a reduction over the images."""
+
+    @staticmethod
+    def forward(ctx, coeffs, basis32, add):
+        K, P = int(basis32.shape[0]), int(basis32[0].numel())
+        n = int(add.shape[0])
+        c = coeffs.detach().to(torch.float64).contiguous()
+        d = add.detach().to(torch.float64).contiguous()
+        out = torch.empty((n,) + tuple(basis32.shape[1:]), dtype=torch.float64, device=c.device)
+        _lib.call('lgb_basis_expand_stack', basis32.data_ptr(), c.data_ptr(), K, P, d.data_ptr(),
+                  n, out.data_ptr(), dv.stream_ptr())
+        ctx.save_for_backward(basis32)
+        ctx.n = n
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        (basis32,) = ctx.saved_tensors
+        K, P = int(basis32.shape[0]), int(basis32[0].numel())
+        g = grad.detach().to(torch.float64).contiguous()
+        out = torch.empty(K, dtype=torch.float64, device=g.device)
+        nb = _lib.load().lgb_basis_project_workspace_size(K)
+        ws = dv.workspace(nb)
+        _lib.call('lgb_basis_project_stack', basis32.data_ptr(), g.data_ptr(), ctx.n, K, P,
+                  out.data_ptr(), ws.data_ptr(), nb, dv.stream_ptr())
+        return out, None, (grad if ctx.needs_input_grad[2] else None)
+
+
 class _SquaredError(torch.autograd.Function):
     """sum (I - T)^2 and its gradient 2 (I - T) dL in one kernel pass each
     (lgb_sq_error, lgb_sq_error_grad), in place of a chain of FP64
@@ -205,9 +237,14 @@ class PhaseRetrieval:
             o = torch.einsum('k,khw->hw', coeffs, self.basis)
         return o if free is None else o + free
 
+    def _stack(self, coeffs, div, free=None):
+        """The OPD maps of all diversity images, [n, H, W] (one batched MFT)."""
+        if self._basis32 is not None and free is None:
+            return _StackedOPD.apply(coeffs, self._basis32, div)
+        return self.opd(coeffs, free).unsqueeze(0) + div
+
     def loss(self, coeffs, free=None):
-        o = self.opd(coeffs, free)
-        stack = o.unsqueeze(0) + torch.stack(self.diversity)   # all images in one batched MFT
+        stack = self._stack(coeffs, torch.stack(self.diversity), free)
         return squared_error(mft_intensity(stack, self.amp, self.g), torch.stack(self.targets))
 
     def graphed_loss(self, coeffs):
@@ -217,8 +254,7 @@ class PhaseRetrieval:
             tgt = torch.stack(self.targets)
 
             def fn(c):
-                o = self.opd(c)
-                return squared_error(mft_intensity(o.unsqueeze(0) + div, self.amp, self.g), tgt)
+                return squared_error(mft_intensity(self._stack(c, div), self.amp, self.g), tgt)
 
             sample = coeffs.detach().clone().requires_grad_(True)
             with fourier.pinned_plans() as pins:

@@ -16,10 +16,12 @@ namespace lgb {
 constexpr int BASIS_MAX_K = 1024;
 constexpr int PROJ_BLOCKS = 76;
 
-// out[p] = sum_k c[k] B[k][p]; c staged in shared memory as FP32
+// out[i][p] = sum_k c[k] B[k][p] + add[i][p] (add null: 0), i < count; c
+// staged in shared memory as FP32
 __global__ void __launch_bounds__(256) basis_expand_kernel(const float* __restrict__ B,
                                                            const double* __restrict__ c, int K,
-                                                           size_t P, double* __restrict__ out) {
+                                                           size_t P, const double* __restrict__ add,
+                                                           int count, double* __restrict__ out) {
   __shared__ float cs[BASIS_MAX_K];
   for (int k = threadIdx.x; k < K; k += blockDim.x) cs[k] = (float)c[k];
   __syncthreads();
@@ -39,7 +41,8 @@ __global__ void __launch_bounds__(256) basis_expand_kernel(const float* __restri
       }
     }
     for (; k < K; ++k) a0 = fmaf(cs[k], __ldg(B + (size_t)k * P + p), a0);
-    out[p] = widen_float(a0 + a1);                 // integer widening: no FP64 pipe
+    const double o = widen_float(a0 + a1);         // integer widening: no FP64 pipe
+    for (int i = 0; i < count; ++i) out[(size_t)i * P + p] = add ? o + add[(size_t)i * P + p] : o;
   }
 }
 
@@ -50,7 +53,7 @@ constexpr int PROJ_KG = 8;        // modes per block of the projection
 // them and keeps one sum per mode; one fixed-order block reduction at the end
 __global__ void __launch_bounds__(256) basis_project_partial_kernel(const float* __restrict__ B,
                                                                     const double* __restrict__ g,
-                                                                    int K, size_t P,
+                                                                    int count, int K, size_t P,
                                                                     double* __restrict__ partial) {
   __shared__ double red[8][PROJ_KG];
   const int k0 = blockIdx.y * PROJ_KG, nk = min(PROJ_KG, K - k0);
@@ -65,7 +68,8 @@ __global__ void __launch_bounds__(256) basis_project_partial_kernel(const float*
 #pragma unroll
   for (int j = 0; j < PROJ_KG; ++j) acc[j] = 0.f;
   for (size_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    const float gv = truncate_double(g[p]);
+    float gv = truncate_double(g[p]);              // the count planes' gradients summed
+    for (int i = 1; i < count; ++i) gv += truncate_double(g[(size_t)i * P + p]);
 #pragma unroll
     for (int j = 0; j < PROJ_KG; ++j)
       if (j < nk) acc[j] = fmaf(__ldg(B + (size_t)(k0 + j) * P + p), gv, acc[j]);
@@ -196,35 +200,49 @@ extern "C" int lgb_sq_error_grad(const double* I, const double* T, size_t n, con
   return LGB_OK;
 }
 
-extern "C" int lgb_basis_expand(const float* basis, const double* coeffs, int K, size_t P,
-                                double* out, lgb_stream stream) {
+extern "C" int lgb_basis_expand_stack(const float* basis, const double* coeffs, int K, size_t P,
+                                      const double* add, int count, double* out,
+                                      lgb_stream stream) {
   LGB_RANGE("lgb_basis_expand");
   LGB_REQUIRE(basis && coeffs && out, LGB_EINVAL, "basis_expand: null pointer");
   LGB_REQUIRE(K >= 1 && K <= BASIS_MAX_K, LGB_EINVAL, "basis_expand: K outside 1..1024");
+  LGB_REQUIRE(count >= 1, LGB_EINVAL, "basis_expand: count < 1");
   if (P == 0) return LGB_OK;
   const int blocks = (int)std::max<size_t>(1, std::min<size_t>((size_t)8 * sm_count(), (P + 255) / 256));
-  basis_expand_kernel<<<blocks, 256, 0, as_stream(stream)>>>(basis, coeffs, K, P, out);
+  basis_expand_kernel<<<blocks, 256, 0, as_stream(stream)>>>(basis, coeffs, K, P, add, count, out);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
+}
+
+extern "C" int lgb_basis_expand(const float* basis, const double* coeffs, int K, size_t P,
+                                double* out, lgb_stream stream) {
+  return lgb_basis_expand_stack(basis, coeffs, K, P, nullptr, 1, out, stream);
 }
 
 extern "C" size_t lgb_basis_project_workspace_size(int K) {
   return K > 0 ? (size_t)K * PROJ_BLOCKS * sizeof(double) : 0;
 }
 
-extern "C" int lgb_basis_project(const float* basis, const double* grad, int K, size_t P,
-                                 double* out, void* workspace, size_t workspace_bytes,
-                                 lgb_stream stream) {
+extern "C" int lgb_basis_project_stack(const float* basis, const double* grad, int count, int K,
+                                       size_t P, double* out, void* workspace,
+                                       size_t workspace_bytes, lgb_stream stream) {
   LGB_RANGE("lgb_basis_project");
   LGB_REQUIRE(basis && grad && out && workspace, LGB_EINVAL, "basis_project: null pointer");
   LGB_REQUIRE(K >= 1 && K <= BASIS_MAX_K, LGB_EINVAL, "basis_project: K outside 1..1024");
+  LGB_REQUIRE(count >= 1, LGB_EINVAL, "basis_project: count < 1");
   LGB_REQUIRE(workspace_bytes >= lgb_basis_project_workspace_size(K), LGB_EWORKSPACE,
               "basis_project: workspace too small");
   double* partial = static_cast<double*>(workspace);
   cudaStream_t s = as_stream(stream);
-  basis_project_partial_kernel<<<dim3(PROJ_BLOCKS, cdiv(K, PROJ_KG)), 256, 0, s>>>(basis, grad, K,
-                                                                                   P, partial);
+  basis_project_partial_kernel<<<dim3(PROJ_BLOCKS, cdiv(K, PROJ_KG)), 256, 0, s>>>(
+      basis, grad, count, K, P, partial);
   basis_project_final_kernel<<<cdiv(K, 4), 128, 0, s>>>(partial, PROJ_BLOCKS, K, out);
   LGB_CUDA(cudaGetLastError());
   return LGB_OK;
+}
+
+extern "C" int lgb_basis_project(const float* basis, const double* grad, int K, size_t P,
+                                 double* out, void* workspace, size_t workspace_bytes,
+                                 lgb_stream stream) {
+  return lgb_basis_project_stack(basis, grad, 1, K, P, out, workspace, workspace_bytes, stream);
 }

@@ -266,3 +266,21 @@ def test_squared_error_matches_torch(cuda_device):
         assert abs(L.item() - R.item()) <= 1e-13 * max(1.0, abs(R.item()))
         assert torch.allclose(gI, I.grad, rtol=1e-15, atol=0)
         assert torch.allclose(gT, T.grad, rtol=1e-15, atol=0)
+
+
+def test_stacked_opd_matches_broadcast_add(cuda_device):
+    # OPD_i = B . c + D_i and dL/dc = B . sum_i dL/dOPD_i in one pass each,
+    # against the modal OPD, a broadcast add and autograd's sum over images
+    rng = np.random.default_rng(8)
+    K, H, W, n = 21, 96, 80, 3
+    B = torch.as_tensor(rng.normal(size=(K, H, W)), device='cuda').float().contiguous()
+    D = torch.as_tensor(rng.normal(size=(n, H, W)) * 1e-7, device='cuda')
+    G = torch.as_tensor(rng.normal(size=(n, H, W)), device='cuda')
+    c1 = torch.as_tensor(rng.normal(size=K) * 1e-8, device='cuda').requires_grad_(True)
+    c2 = c1.detach().clone().requires_grad_(True)
+    s1 = autodiff._StackedOPD.apply(c1, B, D)
+    s2 = autodiff._BasisOPD.apply(c2, B).unsqueeze(0) + D
+    assert torch.equal(s1, s2)
+    (s1 * G).sum().backward()
+    (s2 * G).sum().backward()
+    assert float((c1.grad - c2.grad).abs().max()) <= 1e-6 * float(c2.grad.abs().max())
