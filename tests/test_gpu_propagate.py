@@ -246,6 +246,32 @@ def test_execute_streams_matches_execute(cuda_device):
             assert float((outg - ref).abs().max()) <= 1e-6 * float(ref.abs().max())
 
 
+def test_split_phase_of_a_large_opd(cuda_device):
+    # tens of waves of OPD: the split operand's phase (the float64 OPD split
+    # into a float pair by integer operations, times 1/lambda as a float-float
+    # product, reduced to a cycle) must hold the field to the split's own
+    # precision, as the complex128 plan does
+    H = 128
+    amp = lo.normalize_power(lg.circle((H, H), 60))
+    rho, theta = lg.zernike_coordinates(amp > 0)
+    opd = (30e-6 * lg.zernike(amp > 0, 4, rho=rho, theta=theta)           # ~60 waves P-V
+           + 8e-6 * lg.zernike(amp > 0, 2, rho=rho, theta=theta)
+           + 3e-9 * np.random.default_rng(16).normal(size=(H, H)))
+    wl = np.linspace(500e-9, 700e-9, 6)
+    wt = np.full(len(wl), 1 / len(wl))
+    kw = dict(shape=64, oversample=2)
+    pl = lg.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 120, focal_length=10)
+    ref = lg.broadband_psf(pl, wl, wt, 5e-6, precision='fp64', **kw)
+    po = lo.Pupil(amplitude=amp, opd=opd, pixelscale=1 / 120, focal_length=10)
+    assert lo.peak_normalised_error(ref, lo.broadband_psf(po, wl, wt, 5e-6, **kw)) < 1e-12
+    # fp16 (22 bits, the default split form) holds 1e-6 however far the
+    # defocus lowers the peak; bf16's 16 bits are ~1e-5 of the field, and
+    # against a peak ~1e-3 of the focused one that shows as ~5e-6
+    for prec, tol in (('split-fp16', 1e-6), ('split', 1e-6), ('split-bf16', 2e-5)):
+        img = lg.broadband_psf(pl, wl, wt, 5e-6, precision=prec, **kw)
+        assert lo.peak_normalised_error(img, ref) < tol, prec
+
+
 def test_broadband_many_wavelengths(cuda_device):
     # 520 wavelengths: the phasor operand kernel's blocks then take more than
     # 32 wavelengths each (16 groups at most), so they reload their
