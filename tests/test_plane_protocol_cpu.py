@@ -152,3 +152,32 @@ def test_grism_is_a_deprecated_dispersive_tilt():
     assert any(issubclass(x.category, DeprecationWarning) for x in w)
     d = lg.DispersiveTilt(trace=[0.3, 0], dispersion=[1e-3, 650e-9])
     assert g.__shift__(wavelength=700e-9) == d.__shift__(wavelength=700e-9)
+
+
+def test_shape_and_size_follow_the_mask_hooks():
+    # a plane without a mask reads its mask's shape and rank from the
+    # amplitude; a given mask or an overridden __mask__ (or __amp__) decides
+    # them, as lentil's Plane.shape/size do (lentil/plane.py:173-201)
+    a = np.zeros((40, 30))
+    a[5:20, 3:25] = 1
+    p = lg.Plane(amplitude=a)
+    assert p._mask_is_amplitude() and p.shape == (40, 30) and p.size == 1
+    assert np.array_equal(p.mask, a != 0)
+    m3 = np.stack([a, a, a])
+    q = lg.Plane(amplitude=a, mask=m3)
+    assert not q._mask_is_amplitude() and q.shape == (40, 30) and q.size == 3
+
+    class Masked(lg.Plane):
+        def __mask__(self):
+            return np.ones((2, 8, 9))
+
+    r = Masked(amplitude=np.ones((8, 9)))
+    assert not r._mask_is_amplitude() and r.shape == (8, 9) and r.size == 2
+
+    class Amp(lg.Plane):
+        def __amp__(self):
+            return np.ones((6, 7))
+
+    s = Amp()
+    assert s._mask_is_amplitude() and s.shape == (6, 7) and s.size == 1
+    assert lg.Plane(amplitude=3.0).shape == () and lg.Plane(amplitude=3.0).size == 1
