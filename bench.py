@@ -533,6 +533,13 @@ def run_gpu(args):
                                'the timed region, whose two lanes overlap the kernels of '
                                'consecutive PSFs',
                 'serial_psfs_per_s': psfs / (kernel_region_ms / 1e3),
+                # the timed (two-lane) region itself: algorithmic MFT flops
+                # over its wall time, a lower bound on the kernels' rate (the
+                # step also runs the phasor operand and window kernels)
+                'timed_region_tflops_lower_bound':
+                    (flops_stage1 + flops_stage2) * psfs / (region_ms / 1e3) / 1e12,
+                'timed_region_frac_lower_bound':
+                    (flops_stage1 + flops_stage2) * psfs / (region_ms / 1e3) / 1e12 / peak,
                 'clocks': kclk.summary(),
                 'issued_tflops': issued,
                 'issued_note': 'three split products per algorithmic flop; stage 1 counts '
